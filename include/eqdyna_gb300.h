@@ -1,0 +1,163 @@
+/*
+ * eqdyna_gb300 — C ABI of the GB300 explicit-dynamics hot path of EQdyna.
+ *
+ * The reference time loop is the argument-less Fortran subroutine `driver`
+ * (src/driver.f90:9-34), which mutates module `globalvar` (src/globalvar.f90:81-101).
+ * This ABI replaces lines src/driver.f90:19-29 (velDispUpdate -> storeOffFaultStData ->
+ * zero force -> assembleGlobalKU -> hrglss -> [thermop] -> faulting -> divide by mass).
+ *
+ * Conventions (identical to the Fortran arrays, so a bind(C) interface can pass them as is):
+ *   - every array is column-major with the Fortran shape given in the comment;
+ *   - index VALUES are 1-based (node ids, equation numbers); -1 in eqNumIndexArr is a fixed DOF
+ *     (src/meshgen.f90:667-671); eqNumStartIndexLoc and stressCompIndexArr are 0-based offsets
+ *     exactly as the Fortran stores them;
+ *   - all reals are IEEE binary64, all integers int32 (Fortran integer(kind=4)).
+ * Every entry point returns 0 on success or a positive eqd_status code; none of them exits the
+ * process.  Calls are blocking, not re-entrant on one context, one device per process.
+ */
+#ifndef EQDYNA_GB300_H
+#define EQDYNA_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------------------------ */
+enum eqd_status {
+  EQD_OK = 0,
+  EQD_ERR_INPUT = 1,        /* inconsistent sizes, bad pointer, unsupported option          */
+  EQD_ERR_CUDA = 2,         /* a CUDA runtime call failed                                   */
+  EQD_ERR_OOM = 3,          /* device allocation failed                                     */
+  EQD_ERR_NAN = 4,          /* NaN velocity (src/driver.f90:147-152 stops the run)          */
+  EQD_ERR_UNSUPPORTED = 5,  /* option combination not built                                  */
+  EQD_ERR_NO_DEVICE = 6,    /* no CUDA device visible                                       */
+  EQD_ERR_TIMEOUT = 7,      /* a bounded device wait gave up                                */
+  EQD_ERR_STATE = 8         /* call out of order (step before init, ...)                    */
+};
+
+/* ---- scalar switches and constants read by the hot path ----------------------------------- */
+typedef struct eqd_scalars {
+  double dt;              /* time step (src/readInputFiles.f90:45)                              */
+  double rdampk;          /* stiffness-proportional damping, ALREADY multiplied by dt
+                             (src/readInputFiles.f90:185)                                       */
+  double rdampm;          /* mass-proportional damping (src/globalvar.f90:16, 0 by default)      */
+  double grav, roumax, rhow, gamar; /* gravity body force of the plastic form
+                             (src/assembleGlobalKU.f90:16)                                       */
+  double w;               /* one-point Gauss weight, 8 (src/calcLocalShapeFunc.f90:19)           */
+  double kapa_hg;         /* viscous hourglass coefficient (src/globalvar.f90:30)               */
+  double xsource, ysource, zsource, nucR, nucRuptVel, nucdtau0, nucT; /* nucleation           */
+  double PMLb[8];         /* PML bounds and edge cell sizes (src/meshgen.f90:532-548)           */
+  double vmaxPML, R;      /* PML reference speed and reflection coefficient                    */
+  double ccosphi, sinphi, tv; /* Drucker-Prager constants (src/readInputFiles.f90:182-186)     */
+  double dx;              /* uniform cell size, used by the Q mechanism index                   */
+  double slipRateThres;   /* rupture-time threshold (src/faulting.f90:336)                      */
+  double fric_tp_h;       /* global TP width used by thermop (src/thermop.f90:23-31)            */
+  double time0;           /* timeElapsed before the first step                                   */
+  int32_t C_elastic, C_Q, C_hg, friclaw, TPV, C_nuclea, nucfault, insertFaultType;
+  int32_t nPML, nstep, mode, reserved;
+} eqd_scalars;
+
+/* ---- the Fortran globalvar arrays touched by the time loop --------------------------------- */
+typedef struct eqd_host_arrays {
+  int32_t nnode;          /* totalNumOfNodes                                                     */
+  int32_t nelem;          /* totalNumOfElements                                                  */
+  int32_t neq;            /* totalNumOfEquations                                                 */
+  int32_t size_eqidx;     /* sizeOfEqNumIndexArr                                                 */
+  int64_t size_stress;    /* size of stressArr                                                   */
+  const int32_t *nodeElemIdRelation; /* (8, nelem)                                               */
+  const int32_t *elemTypeArr;        /* (nelem): 1 hex, 2 PML, 11/12 wedge, 13 hex on dip fault  */
+  const int32_t *eqNumIndexArr;      /* (size_eqidx)                                              */
+  const int32_t *eqNumStartIndexLoc; /* (nnode)                                                   */
+  const int32_t *numOfDofPerNodeArr; /* (nnode): 3 or 12                                          */
+  const double *meshCoor;            /* (3, nnode)                                                */
+  const double *eleshp;              /* (3, 8, nelem) global shape-function gradients             */
+  const double *eledet;              /* (nelem)                                                   */
+  const double *mat;                 /* (nelem, 5): vp, vs, rho, lambda, mu — element-major!     */
+  const double *elemass;             /* (24, nelem)                                               */
+  const double *ss;                  /* (6, nelem) hourglass stiffness                            */
+  const double *phi;                 /* (8, 4, nelem) hourglass base vectors                      */
+  double *stressArr;                 /* (size_stress): 12 per element, 21 per PML element         */
+  const int32_t *stressCompIndexArr; /* (nelem)                                                   */
+  double *pstrain;                   /* (nelem)                                                   */
+  const double *eleporep;            /* (nelem)                                                   */
+  const double *nodalMassArr;        /* (neq)                                                     */
+  const double *fnms;                /* (nnode)                                                   */
+  double *v1;                        /* (neq) velocity per equation                               */
+  double *velArr;                    /* (3, nnode)                                                */
+  double *dispArr;                   /* (3, nnode)                                                */
+  double *nodalForceArr;             /* (neq) holds acceleration between steps                    */
+  /* split-node fault */
+  int32_t ntotft, nftmx;
+  const int32_t *nftnd;              /* (ntotft)                                                  */
+  const int32_t *nsmp;               /* (2, nftmx, ntotft): slave, master node ids                */
+  const double *un, *us, *ud;        /* (3, nftmx, ntotft) unit vectors                           */
+  const double *arn;                 /* (nftmx, ntotft) nodal fault area                          */
+  double *fric;                      /* (100, nftmx, ntotft)                                      */
+  double *fnft;                      /* (nftmx, ntotft) rupture time                              */
+  /* stations */
+  int32_t numOnFaultSt;              /* numOfOnFaultStCount                                       */
+  int32_t numOffFaultSt;             /* numOfOffFaultStCount                                      */
+  const int32_t *anonfs;             /* (3, numOnFaultSt)                                          */
+  const int32_t *idhist;             /* (3, 6*numOffFaultSt)                                       */
+  double *onFaultQuantHistSCECForm;  /* (12, nstep, max(1,numOnFaultSt))                          */
+  double *OffFaultStGramSCEC;        /* (6*numOffFaultSt+1, nstep), may be NULL if no station     */
+  double *onFaultTPHist;             /* (2, nftmx, nstep, ntotft), may be NULL unless friclaw>=3  */
+} eqd_host_arrays;
+
+/* ---- precision / solver options of the GPU form ------------------------------------------- */
+enum eqd_precision {
+  EQD_PREC_FP64 = 0,      /* plain form: every operation in binary64 (the drop-in)             */
+  EQD_PREC_FP32 = 1       /* element strain/stress/hourglass in binary32 with compensated
+                             binary32 nodal accumulation; state, fault and Newton in binary64  */
+};
+
+typedef struct eqd_options {
+  int32_t precision;      /* enum eqd_precision                                                */
+  int32_t learned_guess;  /* 1: MLP initial guess for the rate-and-state Newton (friclaw 3/4)  */
+  int32_t record_tp_hist; /* 1: keep onFaultTPHist on the device (forced on for friclaw 5)     */
+  int32_t block_elem;     /* element-kernel block size, 0 = autotuned default                  */
+  int32_t use_graph;      /* 1: capture the multi-step loop in a CUDA graph                    */
+  int32_t device;         /* CUDA device ordinal                                               */
+  int32_t reserved[2];
+} eqd_options;
+
+typedef struct eqd_context eqd_context;
+
+/* Replaces nothing in the reference: called once after init_vel (src/eqdyna3d.f90:70).
+ * Copies every array the hot path reads into device-owned, GPU-laid-out buffers.
+ * The host arrays stay owned by the caller; nothing is retained after return. */
+int eqd_gpu_init(const eqd_scalars *s, const eqd_host_arrays *a, const eqd_options *opt,
+                 eqd_context **ctx);
+
+/* Replaces src/driver.f90:11 and :19-29 for steps nt_begin .. nt_begin+nsteps-1 (1-based).
+ * timeElapsed is advanced by dt per step exactly as the reference accumulates it. */
+int eqd_gpu_step(eqd_context *ctx, int32_t nt_begin, int32_t nsteps);
+
+/* Copies device state back into the caller's arrays (velArr, dispArr, v1, stressArr, pstrain,
+ * fric, fnft, station histories, onFaultTPHist) before the reference's output_* writers
+ * (src/eqdyna3d.f90:75-79).  Pointers that are NULL in `a` are skipped. */
+int eqd_gpu_fetch(eqd_context *ctx, eqd_host_arrays *a);
+
+/* Copies only the fault state (fric, fnft) back — the cheap per-step read of a result. */
+int eqd_gpu_fetch_fault(eqd_context *ctx, double *fric, double *fnft);
+
+/* Frees all device memory of the context (before MPI_Finalize, src/eqdyna3d.f90:86). */
+int eqd_gpu_finalize(eqd_context *ctx);
+
+/* Human-readable text of a status code. */
+const char *eqd_gpu_status_string(int status);
+
+/* Diagnostics: Newton iterations summed over pairs and steps, Newton ivmax hits, element
+ * updates performed, kernel launches issued by the last eqd_gpu_step call. */
+int eqd_gpu_stats(eqd_context *ctx, int64_t *newton_iters, int64_t *newton_maxhits,
+                  int64_t *elem_updates, int64_t *kernel_launches);
+
+/* Current simulation time of the context (timeElapsed). */
+double eqd_gpu_time(eqd_context *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* EQDYNA_GB300_H */

@@ -1,0 +1,88 @@
+"""Unit tests of the host case setup against hand-derived values (CPU only)."""
+import numpy as np
+import pytest
+
+from conftest import golden_path
+
+
+@pytest.fixture(scope="module")
+def tpv8():
+    from eqdyna_gb300.case import Case
+    return Case.from_fixture(golden_path("tpv8"))
+
+
+def test_uniform_cube_tables(tpv8):
+    """For an undistorted cube of side h the one-point tables are: det = (h/2)^3,
+    dN/dx_k = +-1/(4h) (src/calcGlobalShapeFunc.f90), lumped mass rho*h^3/8 per node
+    (src/assembleGlobalMass.f90:376-406) and hourglass vectors equal to the +-1 base patterns
+    (src/assembleGlobalMass.f90:353-373)."""
+    c = tpv8
+    et = c.arrays["elemTypeArr"]
+    conn = c.arrays["nodeElemIdRelation"].reshape(-1, 8)
+    xyz = c.arrays["meshCoor"].reshape(-1, 3)
+    h = 500.0
+    # pick an interior element well inside the uniform region
+    ctr = xyz[conn - 1].mean(axis=1)
+    e = int(np.argmin(np.abs(ctr[:, 0] - 250) + np.abs(ctr[:, 1] - 1250) + np.abs(ctr[:, 2] + 5250)))
+    assert et[e] == 1
+    ext = xyz[conn[e] - 1].max(0) - xyz[conn[e] - 1].min(0)
+    assert np.allclose(ext, h)
+    assert c.arrays["eledet"][e] == pytest.approx((h / 2) ** 3, rel=1e-12)
+    shp = c.arrays["eleshp"].reshape(-1, 8, 3)[e]
+    assert np.allclose(np.abs(shp), 1 / (4 * h), rtol=1e-12)
+    rho = c.arrays["mat"].reshape(5, -1)[2, e]
+    assert np.allclose(c.arrays["elemass"].reshape(-1, 24)[e], rho * h ** 3 / 8, rtol=1e-12)
+    phi = c.arrays["phi"].reshape(-1, 4, 8)[e]
+    assert np.allclose(np.abs(phi), 1.0, atol=1e-9)
+    # hourglass vectors are orthogonal to the linear fields x, y, z and to constants
+    X = xyz[conn[e] - 1]
+    assert np.allclose(phi @ X, 0.0, atol=1e-6)
+    assert np.allclose(phi.sum(axis=1), 0.0, atol=1e-9)
+
+
+def test_mass_and_equation_bookkeeping(tpv8):
+    c = tpv8
+    a = c.arrays
+    ne = c.sizes["nelem"]
+    rho = a["mat"].reshape(5, -1)[2]
+    vol = a["eledet"] * 8.0
+    total = (rho * vol).sum()
+    # every node's fnms sums the element masses (one DOF's worth); totals agree
+    assert a["fnms"].sum() == pytest.approx(total, rel=1e-12)
+    ndof = a["numOfDofPerNodeArr"]
+    assert set(np.unique(ndof)) <= {3, 12}
+    assert a["eqNumIndexArr"].size == ndof.sum()
+    eqs = a["eqNumIndexArr"]
+    assert eqs.max() == c.sizes["neq"]
+    assert np.array_equal(np.sort(eqs[eqs > 0]), np.arange(1, c.sizes["neq"] + 1))
+    # PML elements take 21 stress slots, the others 12
+    et = a["elemTypeArr"]
+    assert a["stressArr"].size == 21 * (et == 2).sum() + 12 * (et != 2).sum()
+    assert ne == (c.dims["nx"] - 1) * (c.dims["ny"] - 1) * (c.dims["nz"] - 1)
+
+
+def test_split_nodes(tpv8):
+    c = tpv8
+    nsmp = c.arrays["nsmp"].reshape(-1, 2)
+    xyz = c.arrays["meshCoor"].reshape(-1, 3)
+    assert np.array_equal(xyz[nsmp[:, 0] - 1], xyz[nsmp[:, 1] - 1])
+    # master nodes are appended after the nx*ny*nz grid nodes (src/meshgen.f90:805)
+    ngrid = c.dims["nx"] * c.dims["ny"] * c.dims["nz"]
+    assert np.array_equal(nsmp[:, 1], ngrid + np.arange(1, len(nsmp) + 1))
+    # elements on the +y side of the fault use master nodes; none uses a slave there
+    conn = c.arrays["nodeElemIdRelation"].reshape(-1, 8)
+    ctr = xyz[conn - 1].mean(axis=1)
+    plus = (ctr[:, 1] > 0) & (ctr[:, 1] < 500)
+    uses_master = np.isin(conn[plus], nsmp[:, 1]).any(axis=1)
+    p = xyz[conn[plus] - 1]
+    on_fault = ((np.abs(p[:, :, 1]) < 1e-9) & (np.abs(p[:, :, 0]) <= 15e3 + 1e-6)
+                & (p[:, :, 2] >= -15e3 - 1e-6))
+    # The reference rewires an element only when its last-created corner node lies below
+    # fxmax + dx (src/meshgen.f90:751-754).  With stretched cells (rat = 1.025) the column just
+    # beyond the +x fault edge is 512.5 m wide, so those elements keep the slave nodes.
+    reachable = p[:, :, 0].max(axis=1) < 15e3 + 500.0 + 1e-5
+    assert np.array_equal(uses_master, on_fault.any(axis=1) & reachable)
+    uses_slave = np.isin(conn[plus], nsmp[:, 0]).any(axis=1)
+    assert np.array_equal(uses_slave, on_fault.any(axis=1) & ~reachable)
+    # fault areas sum to the fault area
+    assert c.arrays["arn"].sum() == pytest.approx(30e3 * 15e3, rel=1e-12)
