@@ -1,0 +1,358 @@
+#!/usr/bin/env python3
+"""Benchmark of the EQdyna explicit-dynamics hot path on GB300.
+
+Metric (BASELINE): element-updates/s = elements advanced x steps / step-loop time.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--config C1] [--precision fp64|fp32]
+                  [--learned 0|1] [--scale S] [--impl ours|reference]
+
+Workload: the configuration the metric is quoted on, C1 (rate-and-state aging law, dx = 100 m,
+20,216,000 elements with a 40-layer PML), synthetic seeded inputs (eqdyna_gb300.configs).
+A "step" is one time step of the hot path over the whole mesh.
+
+value      device time of exactly K steps, CUDA events recorded on the library's own stream
+           around every kernel launch (inputs resident in HBM, working set far above L2).
+e2e        the same metric through the C ABI with host buffers: eqd_gpu_init (host->device copy
+           of every table), then per step eqd_gpu_step + eqd_gpu_fetch_fault (device->host read
+           of the fault state), then eqd_gpu_fetch; host wall clock around all of it.
+roofline   dominant kernel (the element kernel with the largest event time): algorithmic bytes per
+           launch / average launch duration, against the measured HBM copy bandwidth.
+cpu_baseline the oracle (binary64 C++ restatement of the reference step, OpenMP over all host
+           cores) on a bounded sample of the same mesh.
+--impl reference times that CPU implementation alone (the reference's Fortran/MPI/netCDF build
+           is not available on this stack), printing the same JSON line with impl=reference.
+Multi-GPU: the hot path runs one mesh per GPU (no domain decomposition); N ranks run N independent
+           replicas, value = all elements x steps / max time over ranks ("weak").
+"""
+import argparse
+import json
+import os
+import shutil
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "element-updates/s, FP32+learned vs plain FP64 on 1 GB300 at ≤1% slip-rate L2 error"
+UNIT = "element-updates/s"
+
+# Algorithmic bytes per element update (compulsory traffic with per-element stored tables and
+# perfect reuse of nodal data).  Element tables: connectivity, shape gradients, det, lambda/mu,
+# stress read+write, hourglass vectors and stiffness (+ damping / split stress for PML).  Node
+# share: gather of velocity and displacement plus the force scatter.
+ELEM_BYTES = {"fp64": {"interior": 32 + 192 + 8 + 16 + 96 + 256 + 48,
+                       "pml": 32 + 192 + 8 + 16 + 240 + 256 + 48 + 48},
+              "fp32": {"interior": 32 + 96 + 4 + 8 + 48 + 128 + 24,
+                       "pml": 32 + 96 + 4 + 8 + 120 + 128 + 24 + 24}}
+NODE_GATHER_BYTES = {"fp64": 48 + 24, "fp32": 24 + 12}
+PML_NODE_EXTRA = {"fp64": 72, "fp32": 36}
+FP64_FLOPS_PER_ELEM = {"interior": 2 * 423, "pml": 2 * 470}
+
+
+def _peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        if shutil.which("nvidia-smi"):
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def build_case(config, scale, nsteps, workdir):
+    from eqdyna_gb300 import configs
+    from eqdyna_gb300.case import Case
+    configs.CONFIGS[config](workdir, scale=scale, nsteps=nsteps)
+    return Case.from_dir(workdir)
+
+
+def algorithmic_bytes(case, precision):
+    """Per-launch algorithmic bytes of the two element kernels (interior, PML)."""
+    import numpy as np
+    a = case.arrays
+    et = a["elemTypeArr"]
+    conn = a["nodeElemIdRelation"].reshape(-1, 8)
+    nd = a["numOfDofPerNodeArr"]
+    out = {}
+    for name, mask in (("interior", et != 2), ("pml", et == 2)):
+        ne = int(mask.sum())
+        nodes = np.unique(conn[mask]) - 1 if ne else np.zeros(0, dtype=np.int64)
+        npml_nodes = int((nd[nodes] == 12).sum()) if ne else 0
+        out[name] = (ne * ELEM_BYTES[precision][name] + len(nodes) * NODE_GATHER_BYTES[precision]
+                     + npml_nodes * PML_NODE_EXTRA[precision], ne)
+    return out
+
+
+def run_cpu_baseline(case, max_seconds=20.0):
+    from oracle import Oracle
+    nth = os.cpu_count() or 1
+    cpu = case.clone()
+    o = Oracle(cpu, nth)
+    o.step(1)  # first step outside the timing (touches every page)
+    n, t0 = 0, time.perf_counter()
+    while True:
+        o.step(1)
+        n += 1
+        el = time.perf_counter() - t0
+        if el > max_seconds or n >= 50:
+            break
+    o.close()
+    return {"value": case.sizes["nelem"] * n / el, "unit": UNIT, "cores": nth, "kind": "port",
+            "sample": f"{n} time steps of the full mesh ({case.sizes['nelem']} elements) after one "
+                      "untimed step, binary64 C++ restatement of the reference step, OpenMP"}
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allreduce_max(x, world):
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def allreduce_sum(x, world):
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def bench_reference(args, world, rank):
+    """CPU implementation of the reference step (the oracle restatement), all host cores."""
+    if rank != 0:
+        return None
+    with tempfile.TemporaryDirectory(prefix="eqd_bench_") as tmp:
+        case = build_case(args.config, args.scale, max(args.steps + args.warmup + 2, 10), tmp)
+        from oracle import Oracle
+        nth = os.cpu_count() or 1
+        o = Oracle(case, nth)
+        o.step(args.warmup)
+        t0 = time.perf_counter()
+        o.step(args.steps)
+        el = time.perf_counter() - t0
+        ne = case.sizes["nelem"]
+        v = ne * args.steps / el
+        from eqdyna_gb300.configs import WORKLOADS
+        line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic (seeded config generator)",
+                "config": {"workload": f"{args.config}: {WORKLOADS[args.config]}", "elements": ne,
+                           "scale": args.scale},
+                "cpu_baseline": {"value": v, "unit": UNIT, "cores": nth, "kind": "port",
+                                 "sample": f"{args.steps} full-mesh time steps after {args.warmup} "
+                                           "untimed; the reference Fortran build needs MPI and "
+                                           "netCDF, which this stack does not have"},
+                "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        return line
+
+
+def bench_ours(args, world, rank, local):
+    import ctypes as C
+    import numpy as np
+    from eqdyna_gb300 import _native as N
+    from eqdyna_gb300.configs import WORKLOADS
+    from eqdyna_gb300.solver import GpuSolver
+
+    lib = N.gpu_lib()
+    t_setup = time.perf_counter()
+    tmp = tempfile.mkdtemp(prefix="eqd_bench_")
+    total_steps = 2 * (args.steps + args.warmup) + 4
+    case = build_case(args.config, args.scale, total_steps, tmp)
+    shutil.rmtree(tmp, ignore_errors=True)
+    ne = case.sizes["nelem"]
+    host_bytes_in = sum(v.nbytes for k, v in case.arrays.items() if v is not None)
+    setup_s = time.perf_counter() - t_setup
+
+    # ---- end to end through the C ABI with host buffers ----
+    e2e_case = case.clone()
+    fr = np.zeros_like(e2e_case.arrays["fric"])
+    fn = np.zeros_like(e2e_case.arrays["fnft"])
+    barrier(world)
+    t0 = time.perf_counter()
+    s = GpuSolver(e2e_case, precision=args.precision, learned_guess=args.learned, device=local)
+    for _ in range(args.steps):
+        s.step(1)
+        s.fetch_fault(fr, fn)
+    s.fetch()
+    e2e_s = time.perf_counter() - t0
+    s.close()
+    e2e_s = allreduce_max(e2e_s, world)
+    del e2e_case
+    npair = case.npair
+    d2h_per_step = 100 * npair * 8 + npair * 8
+
+    # ---- device-timed steps ----
+    s = GpuSolver(case, precision=args.precision, learned_guess=args.learned, device=local)
+    s.step(args.warmup)
+    s.profile(True, reset=True)
+    barrier(world)
+    with ClockSampler(local) as clk:
+        w0 = time.perf_counter()
+        s.step(args.steps)
+        wall = time.perf_counter() - w0
+    barrier(world)
+    s.profile(False)
+    kt = s.kernel_times()
+    stats = s.stats()
+    step_ms_total = kt["step"][0]
+    dev_s = allreduce_max(step_ms_total / 1e3, world)
+    units = allreduce_sum(float(ne) * args.steps, world)
+    value = units / dev_s
+    s.close()
+
+    # ---- roofline of the dominant kernel ----
+    hbm_peak, peak_kind = _peaks()
+    ab = algorithmic_bytes(case, args.precision)
+    dom = "elem_interior" if kt["elem_interior"][0] >= kt["elem_pml"][0] else "elem_pml"
+    key = "interior" if dom == "elem_interior" else "pml"
+    ms, nl = kt[dom]
+    avg_s = ms / 1e3 / max(nl, 1)
+    bytes_per_launch = ab[key][0]
+    achieved = bytes_per_launch / avg_s / 1e9
+    roofline = {"bound": "hbm", "kernel": f"{dom}_{args.precision}", "achieved": achieved,
+                "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
+                "peak_source": peak_kind, "traffic": None,
+                "algorithmic_bytes_per_launch": bytes_per_launch, "elements_per_launch": ab[key][1],
+                "avg_launch_ms": avg_s * 1e3,
+                "kernel_share": {k: v[0] / step_ms_total for k, v in kt.items() if k != "step"}}
+    if args.precision == "fp64":
+        fp64 = C.c_double()
+        if lib.eqd_gpu_fp64_fma_peak(local, C.byref(fp64)) == 0:
+            fl = FP64_FLOPS_PER_ELEM[key] * ab[key][1] / avg_s / 1e12
+            roofline["fp64"] = {"achieved_tflops": fl, "peak_tflops": fp64.value,
+                                "frac": fl / fp64.value, "flops_per_element": FP64_FLOPS_PER_ELEM[key],
+                                "peak_source": "measured FMA-chain kernel"}
+    cpu = run_cpu_baseline(case, args.cpu_seconds) if (rank == 0 and world == 1 and args.cpu_seconds > 0) else None
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dev_s * 1e3 / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if args.precision == "fp64" else "f32 elements + f64 state",
+            "data": "synthetic (seeded config generator, no external dataset)",
+            "config": {"workload": f"{args.config}: {WORKLOADS[args.config]}", "elements": ne,
+                       "physical_elements": case.dims["n_phys_elem"], "precision": args.precision,
+                       "learned_guess": bool(args.learned), "scale": args.scale,
+                       "l2": f"inputs larger than L2 (element tables alone {host_bytes_in / 1e9:.1f} GB)",
+                       "parallelism": "replicas" if world > 1 else "single GPU",
+                       "setup_s": round(setup_s, 1), "wall_ms_per_step": wall * 1e3 / args.steps},
+            "e2e": {"value": units / e2e_s if world > 1 else ne * args.steps / e2e_s, "unit": UNIT,
+                    "h2d_bytes_per_step": int(host_bytes_in / args.steps),
+                    "d2h_bytes_per_step": int(d2h_per_step + host_bytes_in / args.steps),
+                    "note": "init (every table host->device) + per-step fault-state read + final fetch"},
+            "gpu_launches": int(stats["kernel_launches"]),
+            "newton": {"iters": stats["newton_iters"], "ivmax_hits": stats["newton_maxhits"]},
+            "roofline": roofline, "clocks": clk.summary()}
+    if cpu:
+        line["cpu_baseline"] = cpu
+    return line if rank == 0 else None
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=40)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--config", default="C1")
+    ap.add_argument("--scale", type=float, default=1.0)
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
+    ap.add_argument("--learned", type=int, default=0)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    world, rank, local = dist_setup(args)
+    if args.impl == "reference":
+        line = bench_reference(args, world, rank)
+    else:
+        from eqdyna_gb300 import build
+        if not os.path.exists(build.GPU_LIB):
+            build.build_all()
+        line = bench_ours(args, world, rank, local)
+    if line is not None:
+        print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

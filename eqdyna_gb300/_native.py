@@ -143,12 +143,20 @@ def gpu_lib():
         lib.eqd_gpu_stats.restype = C.c_int
         lib.eqd_gpu_time.argtypes = [C.c_void_p]
         lib.eqd_gpu_time.restype = C.c_double
+        lib.eqd_gpu_profile.argtypes = [C.c_void_p, C.c_int32]
+        lib.eqd_gpu_profile.restype = C.c_int
+        lib.eqd_gpu_kernel_time.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_double),
+                                            C.POINTER(C.c_int64)]
+        lib.eqd_gpu_kernel_time.restype = C.c_int
+        lib.eqd_gpu_fp64_fma_peak.argtypes = [C.c_int32, C.POINTER(C.c_double)]
+        lib.eqd_gpu_fp64_fma_peak.restype = C.c_int
         _gpu_lib = lib
     return _gpu_lib
 
 
 # Entry points the C ABI must export (checked by the CPU test suite).
 GPU_SYMBOLS = ["eqd_gpu_init", "eqd_gpu_step", "eqd_gpu_fetch", "eqd_gpu_fetch_fault",
-               "eqd_gpu_finalize", "eqd_gpu_status_string", "eqd_gpu_stats", "eqd_gpu_time"]
+               "eqd_gpu_finalize", "eqd_gpu_status_string", "eqd_gpu_stats", "eqd_gpu_time",
+               "eqd_gpu_profile", "eqd_gpu_kernel_time", "eqd_gpu_fp64_fma_peak"]
 CASE_SYMBOLS = ["eqd_case_build", "eqd_case_view", "eqd_case_array_len", "eqd_case_dims",
                 "eqd_case_lines", "eqd_case_free", "eqd_case_last_error"]

@@ -1,0 +1,162 @@
+"""Synthetic inputs for the benchmark configurations (no external dataset exists for them).
+
+Each config is written as an ordinary case directory (same files the reference's case.setup
+writes, see eqdyna_gb300.case), seeded with 20261203 + config id.
+
+  C0  slip-weakening, homogeneous half-space, box x[-15,15] y[-10,10] z[-15,0] km, dx = 200 m
+      (150 x 100 x 75 physical + 6 PML layers = 1,469,664 elements), fault x[-12,12] z[-12,0] km,
+      mu_s 0.70 / mu_d 0.50 / Dc 0.3 m, sigma_n -100 MPa, tau0 60 MPa, 3 x 3 km patch at
+      (0, -7.5 km) with tau0 72 MPa, strength barrier on the fault edge, dt 0.008 s, 1000 steps,
+      20 on-fault + 20 surface stations at seeded uniform positions.
+  C1  rate-and-state aging law on the same box at dx = 100 m with a 4 km PML (40 layers,
+      380 x 280 x 190 = 20,216,000 elements), a in [0.008, 0.016] rising smoothly outside a
+      velocity-weakening core (b = 0.012), L 0.02 m, V0 1e-6 m/s, f0 0.6, initial V 1e-12 m/s,
+      241 x 121 fault node pairs, smooth overstress nucleation (TPV104 form), dt 0.004 s,
+      4000 steps.
+  C3  30-degree dipping reverse fault reaching the surface, degenerated wedge elements along
+      the fault, slip law, depth-dependent sigma_n (16.2 MPa/km, capped at 120 MPa),
+      tau0/sigma_n 0.55 with a 2 km circular patch at 0.75.
+
+``scale`` > 1 coarsens dx by that factor (same shapes, fewer elements) for parity tests.
+"""
+import math
+
+import numpy as np
+
+from .case import NC_FIELDS, write_case_dir
+
+SEED0 = 20261203
+
+_NC_INDEX = {k: i for i, (_, k) in enumerate(NC_FIELDS)}
+
+
+def _smooth_box(x, w_flat, w_taper):
+    """1 inside |x| <= w_flat, 0 beyond w_flat + w_taper, C-infinity transition in between
+    (the boxcar of TPV104/105)."""
+    ax = abs(x)
+    if ax <= w_flat:
+        return 1.0
+    if ax >= w_flat + w_taper:
+        return 0.0
+    return 0.5 * (1.0 + math.tanh(w_taper / (ax - w_flat - w_taper) + w_taper / (ax - w_flat)))
+
+
+def _base_params():
+    return dict(mode=1, C_elastic=1, C_nuclea=0, C_degen=0, insertFaultType=0, friclaw=1,
+                ntotft=1, nucfault=1, tpv=0, output_plastic=0, outputGroundMotion=0,
+                outputFinalSurfDisp=0, nx=1, ny=1, nz=1, term=1.0, dt=0.008, nmat=1, n2mat=3,
+                roumax=2670.0, rhow=1000.0, gamar=0.66, rdampk=0.1, vmaxPML=6000.0,
+                xsource=0.0, ysource=0.0, zsource=-7.5e3, nucR=3.0e3, nucRuptVel=-9999.0,
+                nucdtau0=0.0, nucT=1.0, str1ToFaultAngle=45.0, devStrToStrVertRatio=0.33,
+                bulk=0.75, coheplas=5.0e6, strike=270.0, dip=90.0, slipRateThres=0.001,
+                xmin=-15e3, xmax=15e3, ymin=-10e3, ymax=10e3, zmin=-15e3, zmax=0.0,
+                nuni_y_minus=5, nuni_y_plus=5, enlarging_ratio=1.0, dx=200.0, dy=200.0, dz=200.0,
+                fxmin=-12e3, fxmax=12e3, fymin=0.0, fymax=0.0, fzmin=-12e3, fzmax=0.0)
+
+
+def _stations(rng, p, n_on=20, n_off=20):
+    dx = p["dx"]
+    nx = int(round((p["fxmax"] - p["fxmin"]) / dx))
+    nz = int(round((p["fzmax"] - p["fzmin"]) / p["dz"]))
+    on = set()
+    while len(on) < min(n_on, (nx + 1) * (nz + 1)):
+        on.add((int(rng.integers(0, nx + 1)), int(rng.integers(0, nz + 1))))
+    st_on = np.array([[(p["fxmin"] + i * dx) / 1e3, (p["fzmin"] + k * p["dz"]) / 1e3]
+                      for i, k in sorted(on)])
+    # surface stations on grid nodes strictly inside the physical box, off the fault plane; the
+    # grid lines are aligned with the fault edge (x) and the fault plane (y = 0)
+    ilo = int(math.ceil((p["xmin"] - p["fxmin"]) / dx)) + 1
+    ihi = int(math.floor((p["xmax"] - p["fxmin"]) / dx)) - 1
+    jlo = int(math.ceil(p["ymin"] / p["dy"])) + 1
+    jhi = int(math.floor(p["ymax"] / p["dy"])) - 1
+    off = set()
+    while len(off) < n_off:
+        i, j = int(rng.integers(ilo, ihi + 1)), int(rng.integers(jlo, jhi + 1))
+        if j != 0:
+            off.add((i, j))
+    st_off = np.array([[(p["fxmin"] + i * dx) / 1e3, j * p["dy"] / 1e3, 0.0] for i, j in sorted(off)])
+    return st_on, st_off
+
+
+def _fault_grid(p):
+    nfx = int(round((p["fxmax"] - p["fxmin"]) / p["dx"])) + 1
+    nfz = int(round((p["fzmax"] - p["fzmin"]) / p["dz"])) + 1
+    fx = np.linspace(p["fxmin"], p["fxmax"], nfx)
+    fz = np.linspace(p["fzmin"], p["fzmax"], nfz)
+    return fx, fz
+
+
+def config_c0(path, scale=1.0, nsteps=1000):
+    p = _base_params()
+    dx = 200.0 * scale
+    p.update(dx=dx, dy=dx, dz=dx, dt=0.008 * scale, friclaw=1, tpv=0, C_nuclea=0)
+    p["term"] = nsteps * p["dt"]
+    rng = np.random.default_rng(SEED0 + 0)
+    fx, fz = _fault_grid(p)
+    ofv = np.zeros((24, len(fz), len(fx)))
+    F = _NC_INDEX
+    for ix, x in enumerate(fx):
+        for iz, z in enumerate(fz):
+            edge = abs(abs(x) - p["fxmax"]) < 0.01 or abs(z - p["fzmin"]) < 0.01
+            ofv[F[1], iz, ix] = 1000.0 if edge else 0.70
+            ofv[F[2], iz, ix] = 0.50
+            ofv[F[3], iz, ix] = 0.30
+            ofv[F[7], iz, ix] = -100.0e6
+            patch = abs(x) <= 1.5e3 + 1e-6 and abs(z + 7.5e3) <= 1.5e3 + 1e-6
+            ofv[F[8], iz, ix] = 72.0e6 if patch else 60.0e6
+    st_on, st_off = _stations(rng, p)
+    write_case_dir(path, p, [[6000.0, 3464.0, 2670.0]], st_on, st_off, ofv,
+                   gpu_switches={"nPML": 6, "C_hg": 1, "kapa_hg": 0.1})
+    return path
+
+
+def aging_state(a, b, L, V0, f0, tau_over_sigma, V):
+    """State theta for which the regularised aging-law friction equals tau/|sigma| at slip rate V
+    (mu = a asinh(V/(2 V0) exp((f0 + b ln(V0 theta / L)) / a)), solved for theta)."""
+    psi = a * (math.log(2.0 * V0 / V) + _log_sinh(tau_over_sigma / a))
+    return L / V0 * math.exp((psi - f0) / b)
+
+
+def _log_sinh(x):
+    return x + math.log1p(-math.exp(-2 * x)) - math.log(2.0) if x > 20 else math.log(math.sinh(x))
+
+
+def config_c1(path, scale=1.0, nsteps=4000, npml=None):
+    p = _base_params()
+    dx = 100.0 * scale
+    p.update(dx=dx, dy=dx, dz=dx, dt=0.004 * scale, friclaw=3, tpv=104, C_nuclea=1,
+             xsource=0.0, ysource=0.0, zsource=-7.5e3, nucR=3.0e3, nucdtau0=45.0e6, nucT=1.0)
+    p["term"] = nsteps * p["dt"]
+    npml = npml if npml is not None else max(2, int(round(4000.0 / dx)))
+    rng = np.random.default_rng(SEED0 + 1)
+    fx, fz = _fault_grid(p)
+    ofv = np.zeros((24, len(fz), len(fx)))
+    F = _NC_INDEX
+    a0, da, b, L, V0, f0, Vini, sigma, tau = 0.008, 0.008, 0.012, 0.02, 1e-6, 0.6, 1e-12, -100e6, 60e6
+    for ix, x in enumerate(fx):
+        for iz, z in enumerate(fz):
+            core = _smooth_box(x, 9.0e3, 3.0e3) * _smooth_box(-z - 6.0e3, 3.0e3, 3.0e3)
+            a = a0 + da * (1.0 - core)
+            ofv[F[9], iz, ix] = a
+            ofv[F[10], iz, ix] = b
+            ofv[F[11], iz, ix] = L
+            ofv[F[12], iz, ix] = V0
+            ofv[F[13], iz, ix] = f0
+            ofv[F[46], iz, ix] = Vini
+            ofv[F[7], iz, ix] = sigma
+            ofv[F[8], iz, ix] = tau
+            ofv[F[20], iz, ix] = aging_state(a, b, L, V0, f0, tau / abs(sigma), Vini)
+            ofv[F[1], iz, ix], ofv[F[2], iz, ix], ofv[F[3], iz, ix] = 0.7, 0.5, 0.3
+    st_on, st_off = _stations(rng, p)
+    R = {6: 0.01, 10: 0.001, 20: 0.0001}.get(npml, 1e-5 if npml > 20 else 0.001)
+    write_case_dir(path, p, [[6000.0, 3464.0, 2670.0]], st_on, st_off, ofv,
+                   gpu_switches={"nPML": npml, "R": R, "C_hg": 1})
+    return path
+
+
+CONFIGS = {"C0": config_c0, "C1": config_c1}
+
+WORKLOADS = {
+    "C0": "slip-weakening half-space, dx 200 m, 1,469,664 elements (6-layer PML)",
+    "C1": "rate-and-state aging law, dx 100 m, 20,216,000 elements (40-layer PML), learned Newton guess",
+}

@@ -1,0 +1,813 @@
+// C ABI of the GB300 hot path (include/eqdyna_gb300.h): converts the Fortran globalvar arrays
+// into the device layout, drives the per-step kernels (optionally through a CUDA graph) and
+// copies results back into the Fortran arrays.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "eqd_device.cuh"
+#include "mlp_common.cuh"
+
+namespace eqd {
+ElemConst make_elem_const(const Context &c);
+int upload_fp32_tables(Context &c);
+}  // namespace eqd
+
+using namespace eqd;
+
+struct eqd_context {
+  Context c;
+  // host-side maps between the Fortran numbering and the device layout
+  std::vector<int> node_dev, node_orig;          // original node (0-based) <-> device id
+  std::vector<int> gi_orig, gp_orig;             // device element slot -> original element
+  std::vector<int> pair_station_col;             // on-fault station columns
+  std::vector<double> times;                     // timeElapsed after n steps
+  int nftmx = 0;
+};
+
+namespace {
+
+template <typename T>
+int dalloc(Context &c, T *&p, size_t n) {
+  p = nullptr;
+  if (n == 0) return EQD_OK;
+  void *q = nullptr;
+  if (cudaMalloc(&q, n * sizeof(T)) != cudaSuccess) {
+    cudaGetLastError();
+    return EQD_ERR_OOM;
+  }
+  c.allocs.push_back(q);
+  p = static_cast<T *>(q);
+  return EQD_OK;
+}
+
+template <typename T>
+int dupload(Context &c, T *&p, const std::vector<T> &h) {
+  int rc = dalloc(c, p, h.size());
+  if (rc) return rc;
+  if (!h.empty() && cudaMemcpy(p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice) != cudaSuccess)
+    return EQD_ERR_CUDA;
+  return EQD_OK;
+}
+
+#define RC(x)                 \
+  do {                        \
+    int rc_ = (x);            \
+    if (rc_) return rc_;      \
+  } while (0)
+
+// PML damping profile at a point (comdampv, src/comdampv.f90:1-120, for nodes: non-strict
+// corner tests; calcPMLElemKU, src/assembleGlobalKU.f90:139-213, for element centres: strict).
+// Region 14 compares y against xmax in both reference routines; that comparison is kept.
+void pml_damping(const eqd_scalars &s, double x, double y, double z, bool element, double d[3]) {
+  const double xmax0 = s.PMLb[0], xmin0 = s.PMLb[1], ymax0 = s.PMLb[2], ymin0 = s.PMLb[3], zmin0 = s.PMLb[4];
+  auto GE = [&](double p, double q) { return element ? p > q : p >= q; };
+  auto LE = [&](double p, double q) { return element ? p < q : p <= q; };
+  d[0] = d[1] = d[2] = 0.0;
+  const bool below = element ? (z < zmin0) : (z <= zmin0);
+  const bool above = z > zmin0;
+  if (!below && !above) return;
+  d[2] = below ? std::fabs(z - zmin0) : 0.0;
+  if (GE(x, xmax0) && GE(y, ymax0)) { d[0] = std::fabs(x - xmax0); d[1] = std::fabs(y - ymax0); }
+  else if (GE(x, xmax0) && LE(y, ymin0)) { d[0] = std::fabs(x - xmax0); d[1] = std::fabs(y - ymin0); }
+  else if (LE(x, xmin0) && LE(y, ymin0)) { d[0] = std::fabs(x - xmin0); d[1] = std::fabs(y - ymin0); }
+  else if (LE(x, xmin0) && GE(y, xmax0)) { d[0] = std::fabs(x - xmin0); d[1] = std::fabs(y - ymax0); }
+  else if (GE(x, xmax0) && y > ymin0 && y < ymax0) { d[0] = std::fabs(x - xmax0); }
+  else if (LE(y, ymin0) && x > xmin0 && x < xmax0) { d[1] = std::fabs(y - ymin0); }
+  else if (LE(x, xmin0) && y > ymin0 && y < ymax0) { d[0] = std::fabs(x - xmin0); }
+  else if (GE(y, ymax0) && x > xmin0 && x < xmax0) { d[1] = std::fabs(y - ymax0); }
+  const double cell[3] = {s.PMLb[5], s.PMLb[6], s.PMLb[7]};
+  for (int k = 0; k < 3; ++k) {
+    const double delta = s.nPML * cell[k];
+    d[k] = 3.0 * s.vmaxPML / 2.0 / delta * std::log(1.0 / s.R) * std::pow(d[k] / delta, 2.0);
+  }
+}
+
+// Coarse-grained memory-variable constants for one mechanism (qconstant, src/qconstant.f90:3-35,
+// after Liu & Archuleta 2006): relaxation time, weight and the unrelaxed-modulus factor.
+void q_constants(double Q, int k, double &tau, double &wk, double &c1) {
+  static const float taus[8] = {1.72333e-3f, 1.80701e-3f, 5.38887e-3f, 1.99322e-2f,
+                                8.49833e-2f, 4.09335e-1f, 2.05951f, 13.2629f};
+  static const float alf[8] = {1.66958e-2f, 3.81644e-2f, 9.84666e-3f, -1.36803e-2f,
+                               -2.85125e-2f, -5.37309e-2f, -6.65035e-2f, -1.33696e-1f};
+  static const float bet[8] = {8.98758e-2f, 6.84635e-2f, 9.67052e-2f, 1.20172e-1f,
+                               1.30728e-1f, 1.38746e-1f, 1.40705e-1f, 2.14647e-1f};
+  double kap = 3.071f + 1.433f * std::pow(Q, (double)-1.158f) * std::log(Q / 5);
+  kap = kap / (1 + 0.415f * Q);
+  wk = kap * (kap * (double)alf[k - 1] + (double)bet[k - 1]);
+  tau = taus[k - 1];
+  const double w2 = 2.0 * 4.0 * std::atan(1.0);
+  const double den = 1.0 + (tau * w2) * (tau * w2);
+  const double ak0 = 1.0 - wk * 8.0 / den, bk0 = wk * 8.0 * w2 * tau / den;
+  const double r = std::pow(ak0 * ak0 + bk0 * bk0, -0.5);
+  c1 = 0.5 * r * (1.0 + ak0 * r);
+}
+
+int validate(const eqd_scalars *s, const eqd_host_arrays *a) {
+  if (!s || !a) return EQD_ERR_INPUT;
+  if (a->nnode <= 0 || a->nelem <= 0 || a->neq <= 0) return EQD_ERR_INPUT;
+  if (!a->nodeElemIdRelation || !a->elemTypeArr || !a->eqNumIndexArr || !a->eqNumStartIndexLoc ||
+      !a->numOfDofPerNodeArr || !a->meshCoor || !a->eleshp || !a->eledet || !a->mat || !a->ss ||
+      !a->phi || !a->stressArr || !a->stressCompIndexArr || !a->nodalMassArr || !a->fnms ||
+      !a->v1 || !a->velArr || !a->dispArr || !a->nodalForceArr)
+    return EQD_ERR_INPUT;
+  if (s->dt <= 0.0 || s->nstep < 0) return EQD_ERR_INPUT;
+  if (s->C_hg != 1 && s->C_hg != 2) return EQD_ERR_UNSUPPORTED;
+  if (a->ntotft != 1 && a->ntotft != 0) return EQD_ERR_UNSUPPORTED;
+  if (s->friclaw < 1 || s->friclaw > 5) return EQD_ERR_INPUT;
+  return EQD_OK;
+}
+
+int build_device_state(eqd_context &X, const eqd_scalars &s, const eqd_host_arrays &a) {
+  Context &c = X.c;
+  c.sc = s;
+  const int nn = a.nnode, ne = a.nelem;
+  c.nnode = nn;
+  c.nelem = ne;
+  c.neq = a.neq;
+  c.nstep = s.nstep;
+  c.size_stress = a.size_stress;
+  auto eq = [&](int node, int k) -> int {  // 1-based node, 1-based DOF -> 1-based eq or -1
+    const int loc = a.eqNumStartIndexLoc[node - 1] + k;
+    if (loc < 1 || loc > a.size_eqidx) return -2;
+    return a.eqNumIndexArr[loc - 1];
+  };
+  // ---- nodes ----
+  X.node_dev.assign(nn, -1);
+  X.node_orig.clear();
+  for (int j = 0; j < nn; ++j)
+    if (a.numOfDofPerNodeArr[j] == 3) X.node_dev[j] = (int)X.node_orig.size(), X.node_orig.push_back(j);
+  c.n_int = (int)X.node_orig.size();
+  for (int j = 0; j < nn; ++j) {
+    if (a.numOfDofPerNodeArr[j] == 12) X.node_dev[j] = (int)X.node_orig.size(), X.node_orig.push_back(j);
+    else if (a.numOfDofPerNodeArr[j] != 3) return EQD_ERR_INPUT;
+  }
+  c.npml = nn - c.n_int;
+  const int np_ = c.npml;
+  std::vector<double> vel(3 * (size_t)nn), disp(3 * (size_t)nn), F(3 * (size_t)nn, 0.0), inv_mass(nn, 0.0);
+  std::vector<double> F9(9 * (size_t)np_, 0.0), v9(9 * (size_t)np_, 0.0), vh(3 * (size_t)np_, 0.0);
+  std::vector<double> pml_ab(6 * (size_t)np_, 0.0);
+  for (int d = 0; d < nn; ++d) {
+    const int j = X.node_orig[d], node = j + 1;
+    for (int k = 0; k < 3; ++k) disp[k * (size_t)nn + d] = a.dispArr[3 * (size_t)j + k];
+    if (d < c.n_int) {
+      double m = -1;
+      for (int k = 1; k <= 3; ++k) {
+        const int e = eq(node, k);
+        if (e < 1 || e > a.neq) return EQD_ERR_UNSUPPORTED;  // fixed 3-DOF node: not built
+        const double mk = a.nodalMassArr[e - 1];
+        if (k == 1) m = mk;
+        else if (mk != m) return EQD_ERR_UNSUPPORTED;  // anisotropic lumped mass: not built
+        vel[(k - 1) * (size_t)nn + d] = a.v1[e - 1];
+        F[(k - 1) * (size_t)nn + d] = a.nodalForceArr[e - 1];
+      }
+      if (!(m > 0)) return EQD_ERR_INPUT;
+      inv_mass[d] = 1.0 / m;
+    } else {
+      const int p = d - c.n_int;
+      for (int k = 0; k < 3; ++k) vel[k * (size_t)nn + d] = a.velArr[3 * (size_t)j + k];
+      const int e1 = eq(node, 1);
+      if (e1 > 0) {
+        const double m = a.nodalMassArr[e1 - 1];
+        if (!(m > 0)) return EQD_ERR_INPUT;
+        for (int k = 1; k <= 12; ++k) {
+          const int e = eq(node, k);
+          if (e < 1 || e > a.neq) return EQD_ERR_UNSUPPORTED;
+          if (a.nodalMassArr[e - 1] != m) return EQD_ERR_UNSUPPORTED;
+          if (k <= 9) {
+            v9[(k - 1) * (size_t)np_ + p] = a.v1[e - 1];
+            F9[(k - 1) * (size_t)np_ + p] = a.nodalForceArr[e - 1];
+          } else {
+            vh[(k - 10) * (size_t)np_ + p] = a.v1[e - 1];
+            F[(k - 10) * (size_t)nn + d] = a.nodalForceArr[e - 1];
+          }
+        }
+        inv_mass[d] = 1.0 / m;
+        double dm[3];
+        pml_damping(s, a.meshCoor[3 * (size_t)j], a.meshCoor[3 * (size_t)j + 1], a.meshCoor[3 * (size_t)j + 2], false, dm);
+        for (int k = 0; k < 3; ++k) {
+          pml_ab[k * (size_t)np_ + p] = 1.0 / s.dt - dm[k] / 2.0;
+          pml_ab[(3 + k) * (size_t)np_ + p] = 1.0 / (1.0 / s.dt + dm[k] / 2.0);
+        }
+      } else {
+        for (int k = 1; k <= 12; ++k)
+          if (eq(node, k) != -1) return EQD_ERR_UNSUPPORTED;  // partially fixed PML node
+      }
+    }
+  }
+  RC(dupload(c, c.vel, vel));
+  RC(dupload(c, c.disp, disp));
+  RC(dupload(c, c.F, F));
+  RC(dupload(c, c.inv_mass, inv_mass));
+  RC(dupload(c, c.F9, F9));
+  RC(dupload(c, c.v9, v9));
+  RC(dupload(c, c.vh, vh));
+  RC(dupload(c, c.pml_ab, pml_ab));
+  c.f_is_acc = 1;
+
+  // ---- elements ----
+  X.gi_orig.clear();
+  X.gp_orig.clear();
+  for (int e = 0; e < ne; ++e) {
+    const int t = a.elemTypeArr[e];
+    if (t == 1 || t > 10) X.gi_orig.push_back(e);
+    else if (t == 2) X.gp_orig.push_back(e);
+    else return EQD_ERR_INPUT;
+  }
+  const bool body = (s.rdampm != 0.0) || (s.C_elastic == 0);
+  for (int grp = 0; grp < 2; ++grp) {
+    const std::vector<int> &ids = grp == 0 ? X.gi_orig : X.gp_orig;
+    ElemGroup<double> &g = grp == 0 ? c.gi64 : c.gp64;
+    const int m = (int)ids.size();
+    g.ne = m;
+    if (m == 0) continue;
+    std::vector<int> conn(8 * (size_t)m);
+    std::vector<double> shp(24 * (size_t)m), phi(32 * (size_t)m), ss(6 * (size_t)m), detw(m), lam(m), mu(m);
+    const int nstress = grp == 0 ? (s.C_Q == 1 ? 12 : 6) : 15;
+    std::vector<double> st(nstress * (size_t)m), st0, pab, em, hg, porep, pstr, qc;
+    bool any_s0 = false;
+    if (grp == 1) st0.assign(6 * (size_t)m, 0.0), pab.assign(6 * (size_t)m, 0.0);
+    if (body) em.assign(8 * (size_t)m, 0.0);
+    if (s.C_hg == 2) hg.assign(m, 0.0);
+    if (grp == 0 && s.C_elastic == 0) porep.assign(m, 0.0), pstr.assign(m, 0.0);
+    if (grp == 0 && s.C_Q == 1) qc.assign(5 * (size_t)m, 0.0);
+    for (int i = 0; i < m; ++i) {
+      const int e = ids[i];
+      double ctr[3] = {0, 0, 0};
+      for (int q = 0; q < 8; ++q) {
+        const int node = a.nodeElemIdRelation[8 * (size_t)e + q];
+        if (node < 1 || node > nn) return EQD_ERR_INPUT;
+        conn[q * (size_t)m + i] = X.node_dev[node - 1];
+        for (int k = 0; k < 3; ++k) ctr[k] += a.meshCoor[3 * (size_t)(node - 1) + k];
+      }
+      for (double &v : ctr) v /= 8.0;
+      for (int q = 0; q < 24; ++q) shp[q * (size_t)m + i] = a.eleshp[24 * (size_t)e + q];
+      for (int q = 0; q < 32; ++q) phi[q * (size_t)m + i] = a.phi[32 * (size_t)e + q];
+      for (int q = 0; q < 6; ++q) ss[q * (size_t)m + i] = a.ss[6 * (size_t)e + q];
+      detw[i] = a.eledet[e] * s.w;
+      lam[i] = a.mat[3 * (size_t)ne + e];
+      mu[i] = a.mat[4 * (size_t)ne + e];
+      const int64_t base = a.stressCompIndexArr[e];
+      if (base < 0 || base + (grp == 0 ? nstress : 21) > a.size_stress) return EQD_ERR_INPUT;
+      for (int q = 0; q < nstress; ++q) st[q * (size_t)m + i] = a.stressArr[base + q];
+      if (grp == 1) {
+        for (int q = 0; q < 6; ++q) {
+          st0[q * (size_t)m + i] = a.stressArr[base + 15 + q];
+          any_s0 |= (st0[q * (size_t)m + i] != 0.0);
+        }
+        double dm[3];
+        pml_damping(s, ctr[0], ctr[1], ctr[2], true, dm);
+        for (int k = 0; k < 3; ++k) {
+          pab[k * (size_t)m + i] = 1.0 / s.dt - dm[k] / 2.0;
+          pab[(3 + k) * (size_t)m + i] = 1.0 / (1.0 / s.dt + dm[k] / 2.0);
+        }
+      }
+      if (body) {
+        if (!a.elemass) return EQD_ERR_INPUT;
+        for (int q = 0; q < 8; ++q) {
+          const double m0 = a.elemass[24 * (size_t)e + 3 * q];
+          if (a.elemass[24 * (size_t)e + 3 * q + 1] != m0 || a.elemass[24 * (size_t)e + 3 * q + 2] != m0)
+            return EQD_ERR_UNSUPPORTED;
+          em[q * (size_t)m + i] = m0;
+        }
+      }
+      if (s.C_hg == 2)
+        hg[i] = 0.25 * s.kapa_hg * a.mat[2 * (size_t)ne + e] * a.mat[e] * std::pow(a.eledet[e] * s.w, 2.0 / 3.0);
+      if (grp == 0 && s.C_elastic == 0) {
+        porep[i] = a.eleporep ? a.eleporep[e] : 0.0;
+        pstr[i] = a.pstrain ? a.pstrain[e] : 0.0;
+      }
+      if (grp == 0 && s.C_Q == 1) {
+        // Q zone and mechanism index from the element centre (src/calcElemKU.f90:78-103)
+        const double Qs = ctr[2] > -1000.0 ? 10.0 : 50.0, Qp = 2.0 * Qs;
+        const int ip = (int)((ctr[0] - (s.PMLb[1] + s.dx / 2)) / s.dx + 1);
+        const int iq = (int)((ctr[1] - (s.PMLb[3] + s.dx / 2)) / s.dx + 1);
+        const int ir = (int)((ctr[2] - (s.PMLb[4] + s.dx / 2)) / s.dx + 1);
+        const int kk = 1 + ip % 2 + 2 * (iq % 2) + 4 * (ir % 2);
+        if (kk < 1 || kk > 8) return EQD_ERR_INPUT;
+        double tau, wkp, wks, cv, cs;
+        q_constants(Qp, kk, tau, wkp, cv);
+        q_constants(Qs, kk, tau, wks, cs);
+        qc[0 * (size_t)m + i] = std::exp(-s.dt / tau);
+        qc[1 * (size_t)m + i] = mu[i] * cs;
+        qc[2 * (size_t)m + i] = (lam[i] + 2 * mu[i]) * cv;
+        qc[3 * (size_t)m + i] = wkp * 8.0;
+        qc[4 * (size_t)m + i] = wks * 8.0;
+      }
+    }
+    RC(dupload(c, g.conn, conn));
+    RC(dupload(c, g.shp, shp));
+    RC(dupload(c, g.phi, phi));
+    RC(dupload(c, g.ss, ss));
+    RC(dupload(c, g.detw, detw));
+    RC(dupload(c, g.lam, lam));
+    RC(dupload(c, g.mu, mu));
+    RC(dupload(c, g.stress, st));
+    if (grp == 1 && any_s0) RC(dupload(c, g.stress0, st0));
+    if (grp == 1) RC(dupload(c, g.pml_ab, pab));
+    if (body) RC(dupload(c, g.em, em));
+    if (s.C_hg == 2) RC(dupload(c, g.hgcoef, hg));
+    if (!porep.empty()) RC(dupload(c, g.porep, porep));
+    if (!pstr.empty()) RC(dupload(c, g.pstrain, pstr));
+    if (!qc.empty()) RC(dupload(c, g.qcoef, qc));
+  }
+
+  // ---- fault ----
+  const int npair = (a.ntotft >= 1 && a.nftnd) ? a.nftnd[0] : 0;
+  c.npair = npair;
+  X.nftmx = a.nftmx;
+  if (npair > 0) {
+    if (!a.nsmp || !a.un || !a.us || !a.ud || !a.arn || !a.fric || !a.fnft || a.nftmx < npair)
+      return EQD_ERR_INPUT;
+    std::vector<int> ps(npair), pm(npair);
+    std::vector<double> geo(13 * (size_t)npair), fr(100 * (size_t)npair), fn(npair);
+    for (int i = 0; i < npair; ++i) {
+      const int sl = a.nsmp[2 * (size_t)i], ms = a.nsmp[2 * (size_t)i + 1];
+      if (sl < 1 || sl > nn || ms < 1 || ms > nn) return EQD_ERR_INPUT;
+      ps[i] = X.node_dev[sl - 1];
+      pm[i] = X.node_dev[ms - 1];
+      if (ps[i] >= c.n_int || pm[i] >= c.n_int) return EQD_ERR_UNSUPPORTED;  // split node in PML
+      for (int k = 0; k < 3; ++k) {
+        geo[(0 + k) * (size_t)npair + i] = a.un[3 * (size_t)i + k];
+        geo[(3 + k) * (size_t)npair + i] = a.us[3 * (size_t)i + k];
+        geo[(6 + k) * (size_t)npair + i] = a.ud[3 * (size_t)i + k];
+      }
+      geo[9 * (size_t)npair + i] = a.arn[i];
+      geo[10 * (size_t)npair + i] = a.fnms[sl - 1];
+      geo[11 * (size_t)npair + i] = a.fnms[ms - 1];
+      const double *x = a.meshCoor + 3 * (size_t)(sl - 1);
+      geo[12 * (size_t)npair + i] = std::sqrt((x[0] - s.xsource) * (x[0] - s.xsource) +
+                                              (x[1] - s.ysource) * (x[1] - s.ysource) +
+                                              (x[2] - s.zsource) * (x[2] - s.zsource));
+      for (int k = 0; k < 100; ++k) fr[k * (size_t)npair + i] = a.fric[100 * (size_t)i + k];
+      fn[i] = a.fnft[i];
+    }
+    RC(dupload(c, c.pair_s, ps));
+    RC(dupload(c, c.pair_m, pm));
+    RC(dupload(c, c.pair_geo, geo));
+    RC(dupload(c, c.fric, fr));
+    RC(dupload(c, c.fnft, fn));
+    const bool tp = (s.friclaw == 5) || (X.c.opt.record_tp_hist && s.friclaw >= 3);
+    if (tp && s.nstep > 0) {
+      std::vector<double> h(2 * (size_t)npair * s.nstep, 0.0);
+      if (a.onFaultTPHist)
+        for (int t = 0; t < s.nstep; ++t)
+          for (int i = 0; i < npair; ++i)
+            for (int k = 0; k < 2; ++k)
+              h[2 * ((size_t)i + (size_t)npair * t) + k] = a.onFaultTPHist[2 * ((size_t)i + (size_t)a.nftmx * t) + k];
+      RC(dupload(c, c.tp_hist, h));
+    } else if (s.friclaw == 5) {
+      return EQD_ERR_INPUT;
+    }
+  }
+  // ---- stations ----
+  std::vector<PairStation> onst;
+  if (a.numOnFaultSt > 0 && a.anonfs) {
+    for (int j = 0; j < a.numOnFaultSt; ++j)
+      if (a.anonfs[3 * (size_t)j + 2] == 1 && a.anonfs[3 * (size_t)j] >= 1 && a.anonfs[3 * (size_t)j] <= npair)
+        onst.push_back({a.anonfs[3 * (size_t)j] - 1, j});
+  }
+  c.nOnSt = (int)onst.size();
+  RC(dupload(c, c.onst, onst));
+  const int ncol = a.numOnFaultSt > 0 ? a.numOnFaultSt : 1;
+  if (s.nstep > 0) {
+    std::vector<double> oh(12 * (size_t)s.nstep * ncol, 0.0);
+    if (a.onFaultQuantHistSCECForm) std::memcpy(oh.data(), a.onFaultQuantHistSCECForm, oh.size() * sizeof(double));
+    RC(dupload(c, c.onhist, oh));
+  }
+  c.nOffRows = 6 * a.numOffFaultSt;
+  if (c.nOffRows > 0) {
+    if (!a.idhist) return EQD_ERR_INPUT;
+    std::vector<int> rows(3 * (size_t)c.nOffRows);
+    for (int r = 0; r < c.nOffRows; ++r) {
+      const int node = a.idhist[3 * (size_t)r], comp = a.idhist[3 * (size_t)r + 1], type = a.idhist[3 * (size_t)r + 2];
+      if (node < 1 || node > nn || comp < 1 || comp > 3 || (type != 1 && type != 2)) return EQD_ERR_UNSUPPORTED;
+      rows[r] = X.node_dev[node - 1];
+      rows[c.nOffRows + r] = comp - 1;
+      rows[2 * c.nOffRows + r] = type;
+    }
+    RC(dupload(c, c.off_rows, rows));
+    if (s.nstep > 0) {
+      std::vector<double> hh((size_t)(c.nOffRows + 1) * s.nstep, 0.0);
+      if (a.OffFaultStGramSCEC) std::memcpy(hh.data(), a.OffFaultStGramSCEC, hh.size() * sizeof(double));
+      RC(dupload(c, c.offhist, hh));
+    }
+  }
+  // ---- step bookkeeping ----
+  RC(dalloc(c, c.d_nt, 1));
+  RC(dalloc(c, c.d_err, 1));
+  RC(dalloc(c, c.d_stats, 4));
+  EQD_CUDA_OK(cudaMemset(c.d_nt, 0, sizeof(int)));
+  EQD_CUDA_OK(cudaMemset(c.d_err, 0, sizeof(int)));
+  EQD_CUDA_OK(cudaMemset(c.d_stats, 0, 4 * sizeof(unsigned long long)));
+  c.nt = 0;
+  c.time = s.time0;
+  X.times.assign(1, s.time0);
+  return EQD_OK;
+}
+
+int ensure_times(eqd_context &X, int last_nt) {
+  Context &c = X.c;
+  if (last_nt + 1 <= c.times_cap) return EQD_OK;
+  while ((int)X.times.size() < last_nt + 1 + 256) X.times.push_back(X.times.back() + c.sc.dt);
+  double *d = nullptr;
+  if (cudaMalloc(&d, X.times.size() * sizeof(double)) != cudaSuccess) return EQD_ERR_OOM;
+  if (cudaMemcpy(d, X.times.data(), X.times.size() * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess)
+    return EQD_ERR_CUDA;
+  if (c.d_times) {
+    cudaFree(c.d_times);
+    for (auto &p : c.allocs)
+      if (p == c.d_times) p = d;
+  } else {
+    c.allocs.push_back(d);
+  }
+  c.d_times = d;
+  c.times_cap = (int)X.times.size();
+  if (c.graph) {  // the graph captured the old pointer
+    cudaGraphExecDestroy(c.graph);
+    c.graph = nullptr;
+  }
+  return EQD_OK;
+}
+
+// Events of one profiled step: [start, after node, after interior, after PML, after fault].
+constexpr int kEventsPerStep = 5;
+
+int launch_step(Context &c, cudaEvent_t *ev = nullptr) {
+  if (ev) EQD_CUDA_OK(cudaEventRecord(ev[0], c.stream));
+  RC(launch_node_update(c, c.stream));
+  c.f_is_acc = 0;
+  if (ev) EQD_CUDA_OK(cudaEventRecord(ev[1], c.stream));
+  RC(launch_elements(c, c.stream, 0));
+  if (ev) EQD_CUDA_OK(cudaEventRecord(ev[2], c.stream));
+  RC(launch_elements(c, c.stream, 1));
+  if (ev) EQD_CUDA_OK(cudaEventRecord(ev[3], c.stream));
+  RC(launch_fault(c, c.stream));
+  if (ev) EQD_CUDA_OK(cudaEventRecord(ev[4], c.stream));
+  return EQD_OK;
+}
+
+int ensure_events(Context &c, int nsteps) {
+  const size_t need = (size_t)kEventsPerStep * nsteps;
+  while (c.prof_events.size() < need) {
+    cudaEvent_t e;
+    EQD_CUDA_OK(cudaEventCreate(&e));
+    c.prof_events.push_back(e);
+  }
+  return EQD_OK;
+}
+
+// Accumulates the profiled times of the last `nsteps` steps (the stream is synchronised).
+int accumulate_profile(Context &c, int nsteps) {
+  for (int k = 0; k < nsteps; ++k) {
+    cudaEvent_t *ev = &c.prof_events[(size_t)kEventsPerStep * k];
+    float ms[4];
+    for (int q = 0; q < 4; ++q) EQD_CUDA_OK(cudaEventElapsedTime(&ms[q], ev[q], ev[q + 1]));
+    float all;
+    EQD_CUDA_OK(cudaEventElapsedTime(&all, ev[0], ev[4]));
+    c.prof_ms[0] += all;
+    c.prof_launches[0] += 1;
+    for (int q = 0; q < 4; ++q) c.prof_ms[q + 1] += ms[q];
+    c.prof_launches[1] += 1;
+    c.prof_launches[2] += (c.gi64.ne > 0 || c.gi32.ne > 0) ? 1 : 0;
+    c.prof_launches[3] += (c.gp64.ne > 0 || c.gp32.ne > 0) ? 1 : 0;
+    c.prof_launches[4] += (c.npair + c.nOffRows > 0) ? 1 : 0;
+  }
+  return EQD_OK;
+}
+
+// Register-resident FMA chains: 8 independent chains per thread, 2 flops per FMA.
+__global__ void fp64_fma_chain(double *out, int iters, double a, double b) {
+  double x[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) x[k] = threadIdx.x * 1e-9 + k;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) x[k] = fma(x[k], a, b);
+  }
+  double s = 0;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) s += x[k];
+  if (s == 12345.678) out[0] = s;  // keeps the chains live
+}
+
+constexpr int kGraphSteps = 16;
+
+int build_graph(Context &c) {
+  cudaGraph_t g = nullptr;
+  EQD_CUDA_OK(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
+  int rc = EQD_OK;
+  for (int k = 0; k < kGraphSteps && rc == EQD_OK; ++k) rc = launch_step(c);
+  cudaError_t e = cudaStreamEndCapture(c.stream, &g);
+  if (rc) {
+    if (g) cudaGraphDestroy(g);
+    return rc;
+  }
+  if (e != cudaSuccess) return EQD_ERR_CUDA;
+  e = cudaGraphInstantiate(&c.graph, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) {
+    c.graph = nullptr;
+    return EQD_ERR_CUDA;
+  }
+  c.graph_steps = kGraphSteps;
+  return EQD_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *eqd_gpu_status_string(int status) {
+  switch (status) {
+    case EQD_OK: return "ok";
+    case EQD_ERR_INPUT: return "inconsistent or missing input";
+    case EQD_ERR_CUDA: return "CUDA runtime error";
+    case EQD_ERR_OOM: return "device out of memory";
+    case EQD_ERR_NAN: return "NaN velocity";
+    case EQD_ERR_UNSUPPORTED: return "unsupported option combination";
+    case EQD_ERR_NO_DEVICE: return "no CUDA device";
+    case EQD_ERR_TIMEOUT: return "bounded device wait timed out";
+    case EQD_ERR_STATE: return "call out of order";
+    default: return "unknown status";
+  }
+}
+
+int eqd_gpu_init(const eqd_scalars *s, const eqd_host_arrays *a, const eqd_options *opt, eqd_context **out) {
+  if (!out) return EQD_ERR_INPUT;
+  *out = nullptr;
+  int rc = validate(s, a);
+  if (rc) return rc;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return EQD_ERR_NO_DEVICE;
+  }
+  eqd_context *X = new (std::nothrow) eqd_context();
+  if (!X) return EQD_ERR_OOM;
+  Context &c = X->c;
+  if (opt) c.opt = *opt;
+  c.device = c.opt.device;
+  if (c.device < 0 || c.device >= ndev) {
+    delete X;
+    return EQD_ERR_INPUT;
+  }
+  if (cudaSetDevice(c.device) != cudaSuccess) {
+    delete X;
+    return EQD_ERR_CUDA;
+  }
+  c.fp32 = (c.opt.precision == EQD_PREC_FP32);
+  rc = build_device_state(*X, *s, *a);
+  if (!rc && c.fp32) rc = upload_fp32_tables(c);
+  if (!rc && c.opt.learned_guess) rc = mlp_init(c);
+  if (!rc && cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking) != cudaSuccess) rc = EQD_ERR_CUDA;
+  if (rc) {
+    eqd_gpu_finalize(X);
+    return rc;
+  }
+  *out = X;
+  return EQD_OK;
+}
+
+int eqd_gpu_step(eqd_context *X, int32_t nt_begin, int32_t nsteps) {
+  if (!X) return EQD_ERR_STATE;
+  if (nsteps < 0 || nt_begin < 1) return EQD_ERR_INPUT;
+  if (nsteps == 0) return EQD_OK;
+  Context &c = X->c;
+  cudaSetDevice(c.device);
+  RC(ensure_times(*X, nt_begin + nsteps));
+  if (nt_begin != c.nt + 1) {
+    const int prev = nt_begin - 1;
+    EQD_CUDA_OK(cudaMemcpyAsync(c.d_nt, &prev, sizeof(int), cudaMemcpyHostToDevice, c.stream));
+    c.nt = prev;
+  }
+  int done = 0;
+  int64_t launches = 0;
+  const int per_step = 3 + (c.gp64.ne > 0 || c.gp32.ne > 0 ? 1 : 0);
+  if (c.profile) {
+    RC(ensure_events(c, nsteps));
+    for (; done < nsteps; ++done) RC(launch_step(c, &c.prof_events[(size_t)kEventsPerStep * done]));
+    launches = (int64_t)per_step * nsteps;
+  }
+  // the first step after init consumes the stored acceleration and runs outside the graph
+  if (c.f_is_acc && done < nsteps) {
+    RC(launch_step(c));
+    ++done;
+    launches += per_step;
+  }
+  if (c.opt.use_graph && nsteps - done >= kGraphSteps) {
+    if (!c.graph) RC(build_graph(c));
+    while (nsteps - done >= kGraphSteps) {
+      EQD_CUDA_OK(cudaGraphLaunch(c.graph, c.stream));
+      done += kGraphSteps;
+      launches += (int64_t)per_step * kGraphSteps;
+    }
+  }
+  for (; done < nsteps; ++done) {
+    RC(launch_step(c));
+    launches += per_step;
+  }
+  EQD_CUDA_OK(cudaStreamSynchronize(c.stream));
+  EQD_CUDA_OK(cudaGetLastError());
+  int err = 0;
+  EQD_CUDA_OK(cudaMemcpy(&err, c.d_err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (c.profile) RC(accumulate_profile(c, nsteps));
+  c.nt += nsteps;
+  c.time = X->times[c.nt];
+  c.launches_last = launches;
+  c.elem_updates += (int64_t)c.nelem * nsteps;
+  if (err) return EQD_ERR_NAN;
+  return EQD_OK;
+}
+
+int eqd_gpu_fetch_fault(eqd_context *X, double *fric, double *fnft) {
+  if (!X) return EQD_ERR_STATE;
+  Context &c = X->c;
+  const int np = c.npair;
+  if (np == 0) return EQD_OK;
+  cudaSetDevice(c.device);
+  EQD_CUDA_OK(cudaStreamSynchronize(c.stream));
+  std::vector<double> fr(100 * (size_t)np);
+  if (fric) {
+    EQD_CUDA_OK(cudaMemcpy(fr.data(), c.fric, fr.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    for (int i = 0; i < np; ++i)
+      for (int k = 0; k < 100; ++k) fric[100 * (size_t)i + k] = fr[k * (size_t)np + i];
+  }
+  if (fnft) EQD_CUDA_OK(cudaMemcpy(fnft, c.fnft, np * sizeof(double), cudaMemcpyDeviceToHost));
+  return EQD_OK;
+}
+
+int eqd_gpu_fetch(eqd_context *X, eqd_host_arrays *a) {
+  if (!X || !a) return EQD_ERR_STATE;
+  Context &c = X->c;
+  cudaSetDevice(c.device);
+  EQD_CUDA_OK(cudaStreamSynchronize(c.stream));
+  if (a->nnode != c.nnode || a->nelem != c.nelem) return EQD_ERR_INPUT;
+  const int nn = c.nnode, np_ = c.npml;
+  std::vector<double> vel(3 * (size_t)nn), disp(3 * (size_t)nn), F(3 * (size_t)nn), im(nn);
+  std::vector<double> v9(9 * (size_t)np_), vh(3 * (size_t)np_), F9(9 * (size_t)np_);
+  EQD_CUDA_OK(cudaMemcpy(vel.data(), c.vel, vel.size() * 8, cudaMemcpyDeviceToHost));
+  EQD_CUDA_OK(cudaMemcpy(disp.data(), c.disp, disp.size() * 8, cudaMemcpyDeviceToHost));
+  EQD_CUDA_OK(cudaMemcpy(F.data(), c.F, F.size() * 8, cudaMemcpyDeviceToHost));
+  EQD_CUDA_OK(cudaMemcpy(im.data(), c.inv_mass, im.size() * 8, cudaMemcpyDeviceToHost));
+  if (np_ > 0) {
+    EQD_CUDA_OK(cudaMemcpy(v9.data(), c.v9, v9.size() * 8, cudaMemcpyDeviceToHost));
+    EQD_CUDA_OK(cudaMemcpy(vh.data(), c.vh, vh.size() * 8, cudaMemcpyDeviceToHost));
+    EQD_CUDA_OK(cudaMemcpy(F9.data(), c.F9, F9.size() * 8, cudaMemcpyDeviceToHost));
+  }
+  auto eq = [&](int j, int k) { return a->eqNumIndexArr[a->eqNumStartIndexLoc[j] + k - 1]; };
+  for (int d = 0; d < nn; ++d) {
+    const int j = X->node_orig[d];
+    for (int k = 0; k < 3; ++k) {
+      if (a->velArr) a->velArr[3 * (size_t)j + k] = vel[k * (size_t)nn + d];
+      if (a->dispArr) a->dispArr[3 * (size_t)j + k] = disp[k * (size_t)nn + d];
+    }
+    const double sc = c.f_is_acc ? 1.0 : im[d];
+    if (d < c.n_int) {
+      for (int k = 1; k <= 3; ++k) {
+        const int e = eq(j, k);
+        if (a->v1) a->v1[e - 1] = vel[(k - 1) * (size_t)nn + d];
+        if (a->nodalForceArr) a->nodalForceArr[e - 1] = F[(k - 1) * (size_t)nn + d] * sc;
+      }
+    } else if (im[d] != 0.0) {
+      const int p = d - c.n_int;
+      for (int k = 1; k <= 12; ++k) {
+        const int e = eq(j, k);
+        const double v = k <= 9 ? v9[(k - 1) * (size_t)np_ + p] : vh[(k - 10) * (size_t)np_ + p];
+        const double f = k <= 9 ? F9[(k - 1) * (size_t)np_ + p] : F[(k - 10) * (size_t)nn + d];
+        if (a->v1) a->v1[e - 1] = v;
+        if (a->nodalForceArr) a->nodalForceArr[e - 1] = f * sc;
+      }
+    }
+  }
+  // element state
+  if (a->stressArr) {
+    for (int grp = 0; grp < 2; ++grp) {
+      const std::vector<int> &ids = grp == 0 ? X->gi_orig : X->gp_orig;
+      const int m = (int)ids.size();
+      if (m == 0) continue;
+      const int nstress = grp == 0 ? (c.sc.C_Q == 1 ? 12 : 6) : 15;
+      std::vector<double> st(nstress * (size_t)m);
+      if (c.fp32) {
+        std::vector<float> s32(st.size());
+        const ElemGroup<float> &g = grp == 0 ? c.gi32 : c.gp32;
+        EQD_CUDA_OK(cudaMemcpy(s32.data(), g.stress, s32.size() * 4, cudaMemcpyDeviceToHost));
+        for (size_t q = 0; q < st.size(); ++q) st[q] = s32[q];
+      } else {
+        const ElemGroup<double> &g = grp == 0 ? c.gi64 : c.gp64;
+        EQD_CUDA_OK(cudaMemcpy(st.data(), g.stress, st.size() * 8, cudaMemcpyDeviceToHost));
+      }
+      for (int i = 0; i < m; ++i) {
+        const int64_t base = a->stressCompIndexArr[ids[i]];
+        for (int q = 0; q < nstress; ++q) a->stressArr[base + q] = st[q * (size_t)m + i];
+      }
+    }
+  }
+  if (a->pstrain && c.gi64.pstrain) {
+    std::vector<double> ps(c.gi64.ne);
+    EQD_CUDA_OK(cudaMemcpy(ps.data(), c.gi64.pstrain, ps.size() * 8, cudaMemcpyDeviceToHost));
+    for (int i = 0; i < c.gi64.ne; ++i) a->pstrain[X->gi_orig[i]] = ps[i];
+  }
+  RC(eqd_gpu_fetch_fault(X, a->fric, a->fnft));
+  if (c.nstep > 0) {
+    const int ncol = a->numOnFaultSt > 0 ? a->numOnFaultSt : 1;
+    if (a->onFaultQuantHistSCECForm && c.onhist)
+      EQD_CUDA_OK(cudaMemcpy(a->onFaultQuantHistSCECForm, c.onhist, 12 * (size_t)c.nstep * ncol * 8, cudaMemcpyDeviceToHost));
+    if (a->OffFaultStGramSCEC && c.offhist)
+      EQD_CUDA_OK(cudaMemcpy(a->OffFaultStGramSCEC, c.offhist, (size_t)(c.nOffRows + 1) * c.nstep * 8, cudaMemcpyDeviceToHost));
+    if (a->onFaultTPHist && c.tp_hist) {
+      std::vector<double> h(2 * (size_t)c.npair * c.nstep);
+      EQD_CUDA_OK(cudaMemcpy(h.data(), c.tp_hist, h.size() * 8, cudaMemcpyDeviceToHost));
+      for (int t = 0; t < c.nstep; ++t)
+        for (int i = 0; i < c.npair; ++i)
+          for (int k = 0; k < 2; ++k)
+            a->onFaultTPHist[2 * ((size_t)i + (size_t)X->nftmx * t) + k] = h[2 * ((size_t)i + (size_t)c.npair * t) + k];
+    }
+  }
+  return EQD_OK;
+}
+
+int eqd_gpu_finalize(eqd_context *X) {
+  if (!X) return EQD_OK;
+  Context &c = X->c;
+  cudaSetDevice(c.device);
+  if (c.stream) cudaStreamSynchronize(c.stream);
+  if (c.graph) cudaGraphExecDestroy(c.graph);
+  for (cudaEvent_t e : c.prof_events) cudaEventDestroy(e);
+  mlp_free(c);
+  for (void *p : c.allocs) cudaFree(p);
+  if (c.stream) cudaStreamDestroy(c.stream);
+  delete X;
+  return EQD_OK;
+}
+
+int eqd_gpu_stats(eqd_context *X, int64_t *newton_iters, int64_t *newton_maxhits, int64_t *elem_updates,
+                  int64_t *kernel_launches) {
+  if (!X) return EQD_ERR_STATE;
+  Context &c = X->c;
+  unsigned long long st[4] = {0, 0, 0, 0};
+  cudaSetDevice(c.device);
+  EQD_CUDA_OK(cudaStreamSynchronize(c.stream));
+  EQD_CUDA_OK(cudaMemcpy(st, c.d_stats, sizeof(st), cudaMemcpyDeviceToHost));
+  if (newton_iters) *newton_iters = (int64_t)st[0];
+  if (newton_maxhits) *newton_maxhits = (int64_t)st[1];
+  if (elem_updates) *elem_updates = c.elem_updates;
+  if (kernel_launches) *kernel_launches = c.launches_last;
+  return EQD_OK;
+}
+
+double eqd_gpu_time(eqd_context *X) { return X ? X->c.time : 0.0; }
+
+int eqd_gpu_profile(eqd_context *X, int32_t enable) {
+  if (!X) return EQD_ERR_STATE;
+  Context &c = X->c;
+  if (enable == 2) {
+    for (int k = 0; k < 5; ++k) c.prof_ms[k] = 0.0, c.prof_launches[k] = 0;
+    return EQD_OK;
+  }
+  c.profile = enable ? 1 : 0;
+  return EQD_OK;
+}
+
+int eqd_gpu_kernel_time(eqd_context *X, int32_t kind, double *ms, int64_t *launches) {
+  if (!X) return EQD_ERR_STATE;
+  if (kind < 0 || kind > 4) return EQD_ERR_INPUT;
+  if (ms) *ms = X->c.prof_ms[kind];
+  if (launches) *launches = X->c.prof_launches[kind];
+  return EQD_OK;
+}
+
+int eqd_gpu_fp64_fma_peak(int32_t device, double *tflops) {
+  if (!tflops) return EQD_ERR_INPUT;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return EQD_ERR_NO_DEVICE;
+  }
+  EQD_CUDA_OK(cudaSetDevice(device));
+  cudaDeviceProp prop;
+  EQD_CUDA_OK(cudaGetDeviceProperties(&prop, device));
+  double *out = nullptr;
+  EQD_CUDA_OK(cudaMalloc(&out, sizeof(double)));
+  const int threads = 256, blocks = prop.multiProcessorCount * 8, iters = 4096;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  fp64_fma_chain<<<blocks, threads>>>(out, 64, 0.999999, 1e-7);  // warm-up
+  cudaEventRecord(e0);
+  fp64_fma_chain<<<blocks, threads>>>(out, iters, 0.999999, 1e-7);
+  cudaEventRecord(e1);
+  cudaError_t err = cudaEventSynchronize(e1);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  if (err != cudaSuccess || ms <= 0.f) return EQD_ERR_CUDA;
+  *tflops = 2.0 * 8.0 * (double)iters * threads * blocks / (ms * 1e-3) / 1e12;
+  return EQD_OK;
+}
+
+}  // extern "C"

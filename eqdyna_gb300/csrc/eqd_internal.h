@@ -1,0 +1,114 @@
+// Internal definitions shared by the translation units of libeqdyna_gb300.so.
+//
+// Device layout (all arrays structure-of-arrays, component-major: a[c * n + i]):
+//   nodes      device id = 3-DOF nodes first (original order), then 12-DOF PML nodes (original
+//              order); the PML slot of node i is i - n_int, so no lookup table is needed
+//              vel, disp, F  [3][nnode]  velArr, dispArr, force accumulator (DOFs 1-3, or
+//                                         DOFs 10-12 on PML nodes)
+//              inv_mass      [nnode]     1 / nodal mass (0 on fixed nodes)
+//              F9, v9        [9][npml]   split-field force / velocity of PML DOFs 1-9
+//              vh            [3][npml]   v1 of PML DOFs 10-12
+//              pml_a, pml_b  [3][npml]   1/dt - d/2 and 1/(1/dt + d/2) of the node damping
+//   elements   two groups, interior (types 1, 11, 12, 13) and PML (type 2), each in original
+//              order; tables SoA per group: conn[8][ne], shp[24][ne], phi[32][ne], ss[6][ne],
+//              detw[ne] (= eledet * w), lam, mu, stress
+//   fault      one thread per split-node pair, fric[100][np] (fric(k) at row k-1)
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <vector>
+
+#include "eqdyna_gb300.h"
+
+namespace eqd {
+
+// ---- element-group tables (FP64 form keeps double, FP32 form keeps float tables) ----------
+template <typename T>
+struct ElemGroup {
+  int ne = 0;
+  int *conn = nullptr;       // [8][ne] device node ids
+  T *shp = nullptr;          // [24][ne]  (3 * a + k): d N_a / d x_k
+  T *phi = nullptr;          // [32][ne]  (8 * m + a)
+  T *ss = nullptr;           // [6][ne]
+  T *detw = nullptr;         // [ne]
+  T *lam = nullptr, *mu = nullptr;  // [ne]
+  T *stress = nullptr;       // interior: [6][ne] (+[6][ne] Q memory); PML: [15][ne]
+  T *stress0 = nullptr;      // PML: [6][ne] constant initial stress s(16..21), or null
+  T *pml_ab = nullptr;       // PML: [6][ne] a_k = 1/dt - d_k/2, b_k = 1/(1/dt + d_k/2)
+  T *em = nullptr;           // [8][ne] element mass per node (body-force term), or null
+  T *hgcoef = nullptr;       // viscous hourglass coefficient [ne], or null
+  double *pstrain = nullptr; // [ne] plastic strain (interior, plastic form)
+  T *porep = nullptr;        // [ne]
+  T *qcoef = nullptr;        // Q: [5][ne]  exp(-dt/tau), miuu, Mu, wkp, wks
+  int *orig = nullptr;       // [ne] original element id (0-based)
+};
+
+struct PairStation {
+  int pair;      // 0-based pair index
+  int column;    // 0-based station column of onFaultQuantHistSCECForm
+};
+
+struct Context {
+  // sizes
+  int nnode = 0, n_int = 0, npml = 0, nelem = 0, neq = 0;
+  int npair = 0, nstep = 0, nOnSt = 0, nOffRows = 0;
+  int64_t size_stress = 0;
+  eqd_scalars sc{};
+  eqd_options opt{};
+  int fp32 = 0;
+  // node state
+  double *vel = nullptr, *disp = nullptr, *F = nullptr, *inv_mass = nullptr;
+  double *F9 = nullptr, *v9 = nullptr, *vh = nullptr, *pml_ab = nullptr;
+  float *F32 = nullptr;          // FP32 form: compensated force accumulator [2][3][nnode]
+  float *F9_32 = nullptr;        // FP32 form: [2][9][npml]
+  float *vel32 = nullptr;        // FP32 form: [3][nnode] velocity copy
+  float *dl32 = nullptr;         // FP32 form: [3][nnode] disp + rdampk * vel copy
+  int *node_orig = nullptr;      // host only: device id -> original node id (0-based)
+  int *node_dev = nullptr;       // host only: original -> device id
+  // elements
+  ElemGroup<double> gi64, gp64;
+  ElemGroup<float> gi32, gp32;
+  int *elem_type_host = nullptr;
+  // fault
+  int *pair_s = nullptr, *pair_m = nullptr;  // device node ids
+  double *pair_geo = nullptr;   // [13][np]: un(3), us(3), ud(3), arn, mS, mM, radius
+  double *fric = nullptr;       // [100][np]
+  double *fnft = nullptr;       // [np]
+  double *tp_hist = nullptr;    // (2, np, nstep) like onFaultTPHist, or null
+  PairStation *onst = nullptr;  // [nOnSt]
+  double *onhist = nullptr;     // (12, nstep, nOnSt)
+  int *off_rows = nullptr;      // [3][nOffRows]: device node, component (0-2), type (1,2,3)
+  double *offhist = nullptr;    // (nOffRows + 1, nstep)
+  // MLP initial guess (rate-and-state)
+  void *mlp = nullptr;
+  // step bookkeeping
+  int *d_nt = nullptr;          // current step index on the device
+  double *d_times = nullptr;    // [nstep + 2] timeElapsed after nt steps
+  int *d_err = nullptr;         // error word: 1 = NaN velocity
+  unsigned long long *d_stats = nullptr;  // [4]: newton iterations, ivmax hits, ...
+  int nt = 0;                   // steps completed (host mirror)
+  double time = 0.0;
+  int f_is_acc = 0;             // first node update consumes acceleration (from init state)
+  int64_t launches_last = 0;
+  int64_t elem_updates = 0;
+  cudaStream_t stream = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  int graph_steps = 0;
+  int device = 0;
+  int times_cap = 0;            // entries of d_times
+  // profiling (CUDA events around every launch of a step)
+  int profile = 0;
+  std::vector<cudaEvent_t> prof_events;
+  double prof_ms[5] = {0, 0, 0, 0, 0};
+  int64_t prof_launches[5] = {0, 0, 0, 0, 0};
+  std::vector<void *> allocs;   // every device allocation of the context
+};
+
+// ---- launchers implemented in the kernel translation units --------------------------------
+int launch_node_update(Context &c, cudaStream_t s);
+int launch_elements(Context &c, cudaStream_t s, int part = 2);  // 0 interior, 1 PML, 2 both
+int launch_fault(Context &c, cudaStream_t s);
+int mlp_init(Context &c);
+void mlp_free(Context &c);
+
+}  // namespace eqd

@@ -1,0 +1,470 @@
+// Node update and split-node fault kernels.
+//
+// node_update  : the mass division of the previous step (src/driver.f90:29) fused with
+//                velDispUpdate (src/driver.f90:89-155): central-difference update of 3-DOF nodes,
+//                damped split-field update of 12-DOF PML nodes (comdampv precomputed per node),
+//                NaN detection, and zeroing of the force accumulators for this step.
+// fault_kernel : one thread per split-node pair: thermop (src/thermop.f90), faulting
+//                (src/faulting.f90:3-541) with the friction laws (src/fric.f90), station capture
+//                (src/faulting.f90:518-541, src/driver.f90:157-180) and rupture time.
+#include "eqd_device.cuh"
+#include "mlp_common.cuh"
+
+namespace eqd {
+
+namespace {
+
+constexpr int kBlockNode = 256;
+constexpr int kBlockFault = 128;
+
+template <bool F_IS_ACC>
+__global__ void __launch_bounds__(kBlockNode)
+    node_update(double *__restrict__ vel, double *__restrict__ disp, double *__restrict__ F,
+                const double *__restrict__ inv_mass, double *__restrict__ F9,
+                double *__restrict__ v9, double *__restrict__ vh,
+                const double *__restrict__ pml_ab, int nnode, int n_int, int npml, double dt,
+                int *__restrict__ d_nt, int *__restrict__ d_err) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i == 0) *d_nt += 1;
+  if (i >= nnode) return;
+  const double im = inv_mass[i];
+  double v[3];
+  if (i < n_int) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const double f = F[c * nnode + i];
+      const double acc = F_IS_ACC ? f : f * im;
+      v[c] = fma(acc, dt, vel[c * nnode + i]);
+      vel[c * nnode + i] = v[c];
+      disp[c * nnode + i] = fma(v[c], dt, disp[c * nnode + i]);
+      F[c * nnode + i] = 0.0;
+    }
+  } else {
+    const int p = i - n_int;
+    if (im == 0.0) {  // fixed boundary node: eq = -1 (src/driver.f90:141-144)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        v[c] = 0.0;
+        vel[c * nnode + i] = 0.0;
+        disp[c * nnode + i] = 0.0;
+        F[c * nnode + i] = 0.0;
+      }
+#pragma unroll
+      for (int j = 0; j < 9; ++j) F9[j * npml + p] = 0.0;
+    } else {
+      double vs[3] = {0, 0, 0};
+#pragma unroll
+      for (int j = 0; j < 9; ++j) {
+        const int ax = j % 3;
+        const double f = F9[j * npml + p];
+        const double acc = F_IS_ACC ? f : f * im;
+        const double nv = fma(pml_ab[ax * npml + p], v9[j * npml + p], acc) * pml_ab[(3 + ax) * npml + p];
+        v9[j * npml + p] = nv;
+        vs[j / 3] += nv;
+        F9[j * npml + p] = 0.0;
+      }
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const double f = F[c * nnode + i];
+        const double acc = F_IS_ACC ? f : f * im;
+        const double nh = fma(acc, dt, vh[c * npml + p]);
+        vh[c * npml + p] = nh;
+        v[c] = vs[c] + nh;
+        vel[c * nnode + i] = v[c];
+        disp[c * nnode + i] = fma(v[c], dt, disp[c * nnode + i]);
+        F[c * nnode + i] = 0.0;
+      }
+    }
+  }
+  if (isnan(v[0]) || isnan(v[1]) || isnan(v[2])) atomicOr(d_err, 1);
+}
+
+struct FaultArgs {
+  int npair, nnode, nstep, nOnSt, nOffRows, nftmx_tp;
+  int friclaw, TPV, C_nuclea_here, C_elastic, insertFaultType;
+  double dt, nucR, nucRuptVel, nucdtau0, nucT, slipRateThres, fric_tp_h;
+  const int *pair_s, *pair_m;
+  const double *geo;          // [13][np]
+  double *fric;               // [100][np]
+  double *fnft;
+  double *tp_hist;            // (2, np, nstep) or null
+  const PairStation *onst;
+  double *onhist;
+  const int *off_rows;
+  double *offhist;
+  double *F;
+  const double *vel, *disp;
+  const int *d_nt;
+  const double *d_times;
+  unsigned long long *stats;
+  const MlpDevice *mlp;       // learned initial guess, or null
+};
+
+__device__ __forceinline__ void rsf_law(int friclaw, double V2, double &state, const double *fr,
+                                        int np, double dt, double &xmu, double &dxmudv) {
+  // fr(k) == fric(k) of this pair; src/fric.f90:39-95
+#define FR(k) fr[((k)-1) * np]
+  const double A = FR(9), B = FR(10), L = FR(11), f0 = FR(13), V0 = FR(12);
+  if (friclaw == 3) {
+    const double tmpc = 1.0 / (2.0 * V0) * exp((f0 + B * log(V0 * state / L)) / A);
+    const double tmp = (V2 + 1.e-30) * tmpc;
+    xmu = A * log(tmp + sqrt(tmp * tmp + 1.0));
+    dxmudv = A * tmpc / sqrt(1.0 + tmp * tmp);
+    state = L / V2 + (state - L / V2) * exp(-V2 * dt / L);
+  } else {
+    const double fw = FR(14), Vw = FR(15);
+    const double tmpc = 1.0 / (2.0 * V0) * exp(state / A);
+    const double tmp = (V2 + 1.e-30) * tmpc;
+    xmu = A * log(tmp + sqrt(tmp * tmp + 1.0));
+    dxmudv = A * tmpc / sqrt(1.0 + tmp * tmp);
+    const double fLV = f0 - (B - A) * log(V2 / V0);
+    const double r = V2 / Vw, r2 = r * r, r4 = r2 * r2;
+    const double fss = fw + (fLV - fw) / pow(1.0 + r4 * r4, 0.125);
+    const double fssa = fss / A;
+    const double psiss = A * log(2.0 * V0 / V2 * (exp(fssa) - exp(-fssa)) / 2.0);
+    state = psiss + (state - psiss) * exp(-V2 * dt / L);
+  }
+#undef FR
+}
+
+__global__ void __launch_bounds__(kBlockFault) fault_kernel(FaultArgs p) {
+  const int nt = *p.d_nt;
+  const double t = p.d_times[nt];
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int np = p.npair;
+  const int nn = p.nnode;
+  if (tid >= np) {
+    // off-fault station rows (storeOffFaultStData): row 0 is the time
+    const int r = tid - np;
+    if (r <= p.nOffRows && nt >= 1 && nt <= p.nstep && p.offhist) {
+      double val = t;
+      if (r > 0) {
+        const int node = p.off_rows[r - 1], comp = p.off_rows[p.nOffRows + r - 1];
+        const int type = p.off_rows[2 * p.nOffRows + r - 1];
+        val = (type == 1) ? p.disp[comp * nn + node] : p.vel[comp * nn + node];
+      }
+      p.offhist[(size_t)(p.nOffRows + 1) * (nt - 1) + r] = val;
+    }
+    return;
+  }
+  const int i = tid;
+  double *fr = p.fric + i;
+#define FR(k) fr[((k)-1) * np]
+  const double dt = p.dt;
+  const int sl = p.pair_s[i], ms = p.pair_m[i];
+  const double un[3] = {p.geo[0 * np + i], p.geo[1 * np + i], p.geo[2 * np + i]};
+  const double us[3] = {p.geo[3 * np + i], p.geo[4 * np + i], p.geo[5 * np + i]};
+  const double ud[3] = {p.geo[6 * np + i], p.geo[7 * np + i], p.geo[8 * np + i]};
+  const double arn = p.geo[9 * np + i], mS = p.geo[10 * np + i], mM = p.geo[11 * np + i];
+  const double radius = p.geo[12 * np + i];
+
+  // thermal pressurization (src/thermop.f90) — uses the history of previous steps
+  if (p.friclaw == 5 && p.tp_hist) {
+    const double gama = FR(19) / FR(18), omega = FR(16), kapa = FR(17), h2 = 2.0 * p.fric_tp_h * p.fric_tp_h;
+    double tp = 0.0, tt = 0.0;
+    const int jmax = nt - 1 < p.nstep ? nt - 1 : p.nstep;  // history rows that exist
+    for (int j = 1; j <= jmax; ++j) {
+      const double *hh = p.tp_hist + 2 * ((size_t)i + (size_t)np * (j - 1));
+      const double q = fabs(hh[1]) * hh[0];
+      const double s1 = sqrt(4.0 * kapa * (nt - j) * dt + h2);
+      const double s2 = sqrt(4.0 * omega * (nt - j) * dt + h2);
+      const double ker = -kapa / (omega - kapa) / s1 + omega / (omega - kapa) / s2;
+      tp += q * ker * dt;
+      tt += q * (1.0 / s1) * dt;
+    }
+    const double rpi = sqrt(3.14159265358979323846);
+    FR(51) = tp * gama / rpi;
+    FR(52) = tt / FR(18) / rpi + FR(41);
+  }
+
+  // getNsdSlipSliprateTraction (src/faulting.f90:54-134)
+  const double init[3] = {FR(7), FR(8), FR(49)};
+  const double totalMass = (mS + mM) * arn;
+  double q[3][2][3];  // [n|s|d][slave|master][force|vel|disp]
+#pragma unroll
+  for (int j = 0; j < 2; ++j) {
+    const int node = j == 0 ? sl : ms;
+    double x[3][3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      x[0][c] = p.F[c * nn + node];
+      x[1][c] = p.vel[c * nn + node];
+      x[2][c] = p.disp[c * nn + node];
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      q[0][j][k] = x[k][0] * un[0] + x[k][1] * un[1] + x[k][2] * un[2];
+      q[1][j][k] = x[k][0] * us[0] + x[k][1] * us[1] + x[k][2] * us[2];
+      q[2][j][k] = x[k][0] * ud[0] + x[k][1] * ud[1] + x[k][2] * ud[2];
+    }
+  }
+  double slip[4], rate[4], tr[4];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    slip[j] = q[j][1][2] - q[j][0][2];
+    rate[j] = q[j][1][1] - q[j][0][1];
+  }
+  slip[3] = sqrt(slip[0] * slip[0] + slip[1] * slip[1] + slip[2] * slip[2]);
+  rate[3] = sqrt(rate[0] * rate[0] + rate[1] * rate[1] + rate[2] * rate[2]);
+  FR(71) = slip[1];
+  FR(72) = slip[2];
+  FR(73) = slip[0];
+  FR(74) = rate[1];
+  FR(75) = rate[2];
+  if (rate[3] > FR(76)) FR(76) = rate[3];
+  FR(77) = FR(77) + rate[3] * dt;
+  const double mSM = mS * mM;
+  tr[0] = (mSM * ((q[0][1][1] - q[0][0][1]) + (q[0][1][2] - q[0][0][2]) / dt) / dt + mS * q[0][1][0] -
+           mM * q[0][0][0]) / totalMass + init[0] * p.C_elastic;
+  tr[1] = (mSM * (q[1][1][1] - q[1][0][1]) / dt + mS * q[1][1][0] - mM * q[1][0][0]) / totalMass +
+          init[1] * p.C_elastic;
+  tr[2] = (mSM * (q[2][1][1] - q[2][0][1]) / dt + mS * q[2][1][0] - mM * q[2][0][0]) / totalMass +
+          init[2] * p.C_elastic;
+  if (p.friclaw >= 3 && p.C_nuclea_here) {  // rsfNucleation (src/faulting.f90:367-414)
+    double dtau = 0.0, Fn = 0.0, G = 1.0;
+    if (radius < p.nucR) Fn = exp(radius * radius / (radius * radius - p.nucR * p.nucR));
+    if (t <= p.nucT) G = exp((t - p.nucT) * (t - p.nucT) / (t * (t - 2.0 * p.nucT)));
+    if (p.TPV == 105 || p.TPV == 104) {
+      dtau = p.nucdtau0 * Fn * G;
+    } else if (p.TPV == 2802) {
+      if (nt == 1) {
+        FR(81) = p.nucdtau0;
+        const double ttao = sqrt(tr[1] * tr[1] + tr[2] * tr[2]);
+        const double bs = sqrt((rate[1] + FR(26)) * (rate[1] + FR(26)) + (rate[2] + FR(27)) * (rate[2] + FR(27)));
+        FR(20) = FR(9) * log(2.0 * FR(12) / bs * sinh(ttao / fabs(tr[0]) / FR(9)));
+        FR(23) = fabs(tr[0]);
+      }
+      dtau = FR(81) * Fn * G;
+    }
+    tr[1] += dtau;
+  }
+  tr[3] = sqrt(tr[1] * tr[1] + tr[2] * tr[2]);
+
+  double *Fs = p.F + sl, *Fm = p.F + ms;
+  unsigned iters = 0, maxhit = 0;
+  if (p.friclaw <= 2) {
+    // solveSWTW (src/faulting.f90:136-188)
+    double mu;
+    if (p.friclaw == 1) {
+      const double slp = FR(77);
+      mu = 0.0;
+      if (fabs(slp) < 1.0e-10) mu = FR(1);
+      else if (slp < FR(3)) mu = FR(1) - (FR(1) - FR(2)) * slp / FR(3);
+      if (slp >= FR(3)) mu = FR(2);
+    } else {
+      const double tru = t - p.fnft[i];
+      if (tru <= 0.0) mu = FR(1);
+      else if (tru < FR(5)) mu = FR(1) - (FR(1) - FR(2)) * tru / FR(5);
+      else mu = FR(2);
+    }
+    if (p.C_nuclea_here) {  // swtwNucleation (src/faulting.f90:416-443)
+      double trr = 1.0e9;
+      if (radius <= p.nucR) {
+        if (p.TPV == 201 || p.TPV == 36 || p.TPV == 37)
+          trr = (radius + 0.081 * p.nucR * (1.0 / (1.0 - (radius / p.nucR) * (radius / p.nucR)) - 1.0)) / (0.7 * 3464.0);
+        if (p.TPV == 202) trr = radius / p.nucRuptVel;
+      }
+      double tc = 1.0;
+      if (t < trr) tc = 0.0;
+      else if (t < trr + FR(5) && t >= trr) tc = (t - trr) / FR(5);
+      mu = fmin(FR(1) + (FR(2) - FR(1)) * tc, mu);
+    }
+    const double ens = (tr[0] + FR(6) > 0) ? 0.0 : tr[0] + FR(6);
+    const double strength = FR(4) - mu * ens;
+    if (tr[3] > strength) {
+      tr[1] = tr[1] * strength / tr[3];
+      tr[2] = tr[2] * strength / tr[3];
+    }
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      const double xt = (tr[0] * un[j] + tr[1] * us[j] + tr[2] * ud[j]) * arn;
+      const double xi = (init[0] * un[j] + init[1] * us[j] + init[2] * ud[j]) * arn;
+      Fs[j * nn] = Fs[j * nn] + xt - xi * p.C_elastic;
+      Fm[j * nn] = Fm[j * nn] - xt + xi * p.C_elastic;
+    }
+    FR(78) = tr[0];
+    FR(79) = tr[1];
+    FR(80) = tr[2];
+  } else {
+    // solveRSF (src/faulting.f90:190-327)
+    tr[0] += (p.friclaw == 5) ? FR(51) : FR(6);
+    if (p.insertFaultType > 0 && p.C_elastic == 1) {
+      if (tr[0] >= -10.0e6) tr[0] = -10.0e6;
+      else if (tr[0] <= -40.0e6) tr[0] = -40.0e6;
+    }
+    if (tr[0] > 0.0) tr[0] = 0.0;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      slip[j] += FR(25 + j) * t;
+      rate[j] += FR(25 + j);
+    }
+    slip[3] = sqrt(slip[1] * slip[1] + slip[2] * slip[2]);
+    rate[3] = sqrt(rate[1] * rate[1] + rate[2] * rate[2]);
+    double vt = rate[3];
+    const double thpc0 = FR(23);
+    const double L = FR(11);
+    {
+      const double thdot = -vt / L * (FR(23) - fabs(tr[0]));
+      FR(23) = FR(23) + thdot * dt;
+      FR(24) = thdot;
+    }
+    const double state0 = FR(20);
+    double xmu, dxmudv;
+    {
+      double st = FR(20);
+      rsf_law(p.friclaw, vt, st, fr, np, dt, xmu, dxmudv);
+      FR(20) = st;
+    }
+    const double taoc_old = (p.friclaw == 5) ? FR(4) - xmu * tr[0] : xmu * thpc0;
+    const double mr = mM * mS / (mM + mS);
+    const double Tc = arn * dt / mr;
+    double trial[4];
+#pragma unroll
+    for (int j = 1; j <= 2; ++j) trial[j] = tr[j] - taoc_old * 0.5 * (rate[j] / rate[3]) + FR(25 + j) / Tc;
+    trial[3] = sqrt(trial[1] * trial[1] + trial[2] * trial[2]);
+    // learned initial guess for the Newton iteration (same residual, same exit test)
+    if (p.mlp) {
+      const double feat[6] = {log(vt), state0, tr[0], trial[3], FR(9), FR(10)};
+      const double g = mlp_guess(*p.mlp, feat);
+      if (g > 0.0 && isfinite(g)) vt = g;
+    }
+    // NewtonRaphson (src/faulting.f90:459-516)
+    double stateTmp = state0, thTmp = thpc0, taoc_new = 0.0;
+    int iv;
+    for (iv = 1; iv <= 20; ++iv) {
+      stateTmp = state0;
+      rsf_law(p.friclaw, vt, stateTmp, fr, np, dt, xmu, dxmudv);
+      double rsfeq, dr;
+      if (p.friclaw < 5) {
+        thTmp = thpc0;
+        const double thdot = -vt / L * (thTmp - fabs(tr[0]));
+        thTmp = thTmp + thdot * dt;
+        taoc_new = xmu * thTmp;
+        rsfeq = vt + Tc * (taoc_new * 0.5 - trial[3]);
+        dr = 1.0 + Tc * (dxmudv * thTmp) * 0.5;
+      } else {
+        taoc_new = FR(4) - xmu * fmin(tr[0], 0.0);
+        rsfeq = vt + Tc * (taoc_new * 0.5 - trial[3]);
+        dr = 1.0 + Tc * (-dxmudv * fmin(tr[0], 0.0)) * 0.5;
+      }
+      if (fabs(rsfeq / dr) < 1.e-14 * fabs(vt) && fabs(rsfeq) < 1.e-6 * fabs(vt)) break;
+      const double vn = vt - rsfeq / dr;
+      vt = (vn <= 0.0) ? vt / 2.0 : vn;
+    }
+    iters = iv > 20 ? 20 : iv;
+    maxhit = iv > 20 ? 1 : 0;
+    if (p.TPV == 105 && vt < FR(46)) vt = FR(46);
+    FR(20) = stateTmp;
+    FR(23) = thTmp;
+#pragma unroll
+    for (int j = 1; j <= 2; ++j) tr[j] = taoc_old * 0.5 * (rate[j] / rate[3]) + taoc_new * 0.5 * (trial[j] / trial[3]);
+    FR(78) = tr[0];
+    FR(79) = tr[1];
+    FR(80) = tr[2];
+    FR(47) = vt;
+    FR(48) = sqrt(tr[1] * tr[1] + tr[2] * tr[2]);
+    if (p.tp_hist && nt >= 1 && nt <= p.nstep) {
+      double *hh = p.tp_hist + 2 * ((size_t)i + (size_t)np * (nt - 1));
+      hh[0] = FR(47);
+      hh[1] = FR(48);
+    }
+    const double acc[3] = {-rate[0] / dt - slip[0] / dt / dt, (vt * (trial[1] / trial[3]) - rate[1]) / dt,
+                           (vt * (trial[2] / trial[3]) - rate[2]) / dt};
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      const double xa = acc[0] * un[j] + acc[1] * us[j] + acc[2] * ud[j];
+      const double R = Fs[j * nn] + Fm[j * nn];
+      Fs[j * nn] = (-xa + R / mM) * mr;
+      Fm[j * nn] = (xa + R / mS) * mr;
+      FR(31 + j) = p.vel[j * nn + ms] + (xa + R / mS) * dt;
+      FR(34 + j) = p.vel[j * nn + sl] + (-xa + R / mM) * dt;
+    }
+  }
+  if (p.friclaw >= 3) {
+    warp_count_add(p.stats + 0, iters);
+    warp_count_add(p.stats + 1, maxhit);
+  }
+  // storeOnFaultStationQuantSCEC
+  if (nt >= 1 && nt <= p.nstep) {
+    for (int j = 0; j < p.nOnSt; ++j) {
+      if (p.onst[j].pair != i) continue;
+      double *h = p.onhist + 12 * ((size_t)(nt - 1) + (size_t)p.nstep * p.onst[j].column);
+      h[0] = t;
+      h[1] = rate[1];
+      h[2] = rate[2];
+      h[3] = FR(20);
+      h[4] = slip[1];
+      h[5] = slip[2];
+      h[6] = slip[0];
+      h[7] = tr[1];
+      h[8] = tr[2];
+      h[9] = tr[0];
+      h[10] = FR(51) + FR(42);
+      h[11] = FR(52);
+    }
+  }
+  // storeRuptureTime
+  if (p.fnft[i] > 5000.0 && rate[3] >= p.slipRateThres) p.fnft[i] = t;
+#undef FR
+}
+
+}  // namespace
+
+int launch_node_update(Context &c, cudaStream_t s) {
+  const int grid = (c.nnode + kBlockNode - 1) / kBlockNode;
+  if (c.f_is_acc)
+    node_update<true><<<grid, kBlockNode, 0, s>>>(c.vel, c.disp, c.F, c.inv_mass, c.F9, c.v9, c.vh,
+                                                  c.pml_ab, c.nnode, c.n_int, c.npml, c.sc.dt,
+                                                  c.d_nt, c.d_err);
+  else
+    node_update<false><<<grid, kBlockNode, 0, s>>>(c.vel, c.disp, c.F, c.inv_mass, c.F9, c.v9, c.vh,
+                                                   c.pml_ab, c.nnode, c.n_int, c.npml, c.sc.dt,
+                                                   c.d_nt, c.d_err);
+  return cudaGetLastError() == cudaSuccess ? EQD_OK : EQD_ERR_CUDA;
+}
+
+int launch_fault(Context &c, cudaStream_t s) {
+  const int nthreads = c.npair + (c.nOffRows > 0 ? c.nOffRows + 1 : 0);
+  if (nthreads == 0) return EQD_OK;
+  FaultArgs p;
+  p.npair = c.npair;
+  p.nnode = c.nnode;
+  p.nstep = c.nstep;
+  p.nOnSt = c.nOnSt;
+  p.nOffRows = c.nOffRows;
+  p.nftmx_tp = c.npair;
+  p.friclaw = c.sc.friclaw;
+  p.TPV = c.sc.TPV;
+  p.C_nuclea_here = (c.sc.C_nuclea == 1 && c.sc.nucfault == 1) ? 1 : 0;
+  p.C_elastic = c.sc.C_elastic;
+  p.insertFaultType = c.sc.insertFaultType;
+  p.dt = c.sc.dt;
+  p.nucR = c.sc.nucR;
+  p.nucRuptVel = c.sc.nucRuptVel;
+  p.nucdtau0 = c.sc.nucdtau0;
+  p.nucT = c.sc.nucT;
+  p.slipRateThres = c.sc.slipRateThres;
+  p.fric_tp_h = c.sc.fric_tp_h;
+  p.pair_s = c.pair_s;
+  p.pair_m = c.pair_m;
+  p.geo = c.pair_geo;
+  p.fric = c.fric;
+  p.fnft = c.fnft;
+  p.tp_hist = c.tp_hist;
+  p.onst = c.onst;
+  p.onhist = c.onhist;
+  p.off_rows = c.off_rows;
+  p.offhist = c.offhist;
+  p.F = c.F;
+  p.vel = c.vel;
+  p.disp = c.disp;
+  p.d_nt = c.d_nt;
+  p.d_times = c.d_times;
+  p.stats = c.d_stats;
+  p.mlp = static_cast<const MlpDevice *>(mlp_device_params(c));
+  const int grid = (nthreads + kBlockFault - 1) / kBlockFault;
+  fault_kernel<<<grid, kBlockFault, 0, s>>>(p);
+  return cudaGetLastError() == cudaSuccess ? EQD_OK : EQD_ERR_CUDA;
+}
+
+}  // namespace eqd

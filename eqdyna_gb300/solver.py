@@ -1,0 +1,106 @@
+"""Python host API over the C ABI: the call sequence the Fortran driver makes.
+
+    solver = GpuSolver(case)            # eqd_gpu_init   (after init_vel, src/eqdyna3d.f90:70)
+    solver.step(n)                      # eqd_gpu_step   (src/driver.f90:19-29, n steps)
+    solver.fetch()                      # eqd_gpu_fetch  (before output_*, src/eqdyna3d.f90:75)
+    solver.close()                      # eqd_gpu_finalize
+
+The solver writes results back into the Case's own numpy arrays (the Fortran globalvar view).
+There is no CPU fallback: without the built library or a CUDA device the constructor raises.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _native as N
+
+PRECISIONS = {"fp64": N.PREC_FP64, "fp32": N.PREC_FP32}
+
+
+class GpuSolver:
+    def __init__(self, case, precision="fp64", learned_guess=False, use_graph=True, device=0,
+                 record_tp_hist=False):
+        self.lib = N.gpu_lib()
+        self.case = case
+        self._ha = case.host_arrays()
+        opt = N.EqdOptions()
+        opt.precision = PRECISIONS[precision]
+        opt.learned_guess = int(bool(learned_guess))
+        opt.record_tp_hist = int(bool(record_tp_hist))
+        opt.use_graph = int(bool(use_graph))
+        opt.device = int(device)
+        self._opt = opt
+        h = C.c_void_p()
+        rc = self.lib.eqd_gpu_init(C.byref(case.scalars), C.byref(self._ha), C.byref(opt), C.byref(h))
+        if rc != 0:
+            raise N.EqdError(rc, "eqd_gpu_init")
+        self._h = h
+        self.nt = 0
+        self.precision = precision
+
+    def step(self, nsteps=1):
+        rc = self.lib.eqd_gpu_step(self._h, self.nt + 1, int(nsteps))
+        if rc != 0:
+            raise N.EqdError(rc, "eqd_gpu_step")
+        self.nt += int(nsteps)
+
+    def run(self):
+        self.step(self.case.nstep - self.nt)
+
+    def fetch(self):
+        rc = self.lib.eqd_gpu_fetch(self._h, C.byref(self._ha))
+        if rc != 0:
+            raise N.EqdError(rc, "eqd_gpu_fetch")
+
+    def fetch_fault(self, fric=None, fnft=None):
+        fric = self.case.arrays["fric"] if fric is None else fric
+        fnft = self.case.arrays["fnft"] if fnft is None else fnft
+        rc = self.lib.eqd_gpu_fetch_fault(self._h, fric.ctypes.data_as(N.c_double_p),
+                                          fnft.ctypes.data_as(N.c_double_p))
+        if rc != 0:
+            raise N.EqdError(rc, "eqd_gpu_fetch_fault")
+
+    def stats(self):
+        vals = [C.c_int64() for _ in range(4)]
+        rc = self.lib.eqd_gpu_stats(self._h, *[C.byref(v) for v in vals])
+        if rc != 0:
+            raise N.EqdError(rc, "eqd_gpu_stats")
+        return dict(zip(["newton_iters", "newton_maxhits", "elem_updates", "kernel_launches"],
+                        [v.value for v in vals]))
+
+    def profile(self, enable=True, reset=False):
+        if reset:
+            self.lib.eqd_gpu_profile(self._h, 2)
+        self.lib.eqd_gpu_profile(self._h, 1 if enable else 0)
+
+    KERNEL_KINDS = {"step": 0, "node_update": 1, "elem_interior": 2, "elem_pml": 3, "fault": 4}
+
+    def kernel_times(self):
+        """{kind: (total ms, launches)} accumulated while profiling."""
+        out = {}
+        for name, k in self.KERNEL_KINDS.items():
+            ms, n = C.c_double(), C.c_int64()
+            self.lib.eqd_gpu_kernel_time(self._h, k, C.byref(ms), C.byref(n))
+            out[name] = (ms.value, n.value)
+        return out
+
+    @property
+    def time(self):
+        return self.lib.eqd_gpu_time(self._h)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self.lib.eqd_gpu_finalize(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -157,6 +157,19 @@ int eqd_gpu_stats(eqd_context *ctx, int64_t *newton_iters, int64_t *newton_maxhi
 /* Current simulation time of the context (timeElapsed). */
 double eqd_gpu_time(eqd_context *ctx);
 
+/* Timing of subsequent eqd_gpu_step calls: with enable = 1 every step records CUDA events on
+ * the library's stream around each kernel launch (the step loop is issued as plain stream
+ * launches, no graph, while enabled).  enable = 0 stops and enable = 2 resets the totals. */
+int eqd_gpu_profile(eqd_context *ctx, int32_t enable);
+
+/* Milliseconds and launch count accumulated while profiling, per kind:
+ * 0 whole steps, 1 node update, 2 interior elements, 3 PML elements, 4 fault + stations. */
+int eqd_gpu_kernel_time(eqd_context *ctx, int32_t kind, double *ms, int64_t *launches);
+
+/* Measured binary64 fused-multiply-add throughput of a device (TFLOP/s, 2 flops per FMA),
+ * from a register-resident FMA chain kernel; used as the compute roofline of the FP64 form. */
+int eqd_gpu_fp64_fma_peak(int32_t device, double *tflops);
+
 #ifdef __cplusplus
 }
 #endif

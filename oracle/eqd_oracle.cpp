@@ -167,7 +167,7 @@ int vel_disp_update(Oracle &o) {
 void store_off_fault(Oracle &o, int nt) {
   View v(o);
   const int n = o.a.numOffFaultSt * 6;
-  if (n <= 0 || !o.a.OffFaultStGramSCEC) return;
+  if (n <= 0 || !o.a.OffFaultStGramSCEC || nt < 1 || nt > o.s.nstep) return;  // rows exist for 1..nstep
   double *g = o.a.OffFaultStGramSCEC + (size_t)(n + 1) * (nt - 1);
   g[0] = o.timeElapsed;
   for (int i = 1; i <= n; ++i) {
@@ -721,7 +721,7 @@ void fault_pair(Oracle &o, int i, int nt) {
     for (int j = 0; j < 3; ++j) fr[78 + j] = tr[j];
     fr[47] = vt;
     fr[48] = std::sqrt(tr[1] * tr[1] + tr[2] * tr[2]);
-    if (o.a.onFaultTPHist) {
+    if (o.a.onFaultTPHist && nt >= 1 && nt <= s.nstep) {
       double *h = o.a.onFaultTPHist + 2 * ((size_t)(i - 1) + (size_t)o.a.nftmx * (nt - 1));
       h[0] = fr[47];
       h[1] = fr[48];
@@ -743,7 +743,7 @@ void fault_pair(Oracle &o, int i, int nt) {
     }
   }
   // storeOnFaultStationQuantSCEC, :518-541
-  for (int j = 1; j <= o.a.numOnFaultSt; ++j) {
+  for (int j = 1; j <= o.a.numOnFaultSt && nt >= 1 && nt <= s.nstep; ++j) {
     if (o.a.anonfs[3 * (j - 1)] == i && o.a.anonfs[3 * (j - 1) + 2] == 1) {
       double *h = o.a.onFaultQuantHistSCECForm + 12 * ((size_t)(nt - 1) + (size_t)s.nstep * (j - 1));
       h[0] = t;
@@ -776,7 +776,8 @@ void thermop(Oracle &o, int nt) {
     double *fr = &v.fric(1, i) - 1;
     const double gama = fr[19] / fr[18], omega = fr[16], kapa = fr[17];
     double tmp = 0.0;
-    for (int j = 1; j <= nt - 1; ++j) {
+    const int jmax = nt - 1 < s.nstep ? nt - 1 : s.nstep;
+    for (int j = 1; j <= jmax; ++j) {
       double ker = -kapa / (omega - kapa) / std::pow(4.0 * kapa * (nt - j) * dt + 2.0 * h * h, 0.5);
       ker = ker + omega / (omega - kapa) / std::pow(4.0 * omega * (nt - j) * dt + 2.0 * h * h, 0.5);
       const double *hh = o.a.onFaultTPHist + 2 * ((size_t)(i - 1) + (size_t)o.a.nftmx * (j - 1));
@@ -784,7 +785,7 @@ void thermop(Oracle &o, int nt) {
     }
     o.patnode[i - 1] = tmp * gama / std::pow(pi, 0.5);
     tmp = 0.0;
-    for (int j = 1; j <= nt - 1; ++j) {
+    for (int j = 1; j <= jmax; ++j) {
       const double ker = 1.0 / std::pow(4.0 * kapa * (nt - j) * dt + 2.0 * h * h, 0.5);
       const double *hh = o.a.onFaultTPHist + 2 * ((size_t)(i - 1) + (size_t)o.a.nftmx * (j - 1));
       tmp = tmp + std::fabs(hh[1]) * hh[0] * ker * dt;

@@ -1,0 +1,152 @@
+"""GPU binary64 form vs the oracle (and vs the reference golden), through the C ABI.
+
+Bar (the benchmark spec): relative L2 <= 1e-9 on slip, slip rate and station velocities, rupture time
+within one time step.  Element forces are summed into nodes in a different order than the
+reference (and atomically), so agreement is to round-off, not bitwise.
+"""
+import numpy as np
+import pytest
+
+from conftest import golden_path, nthreads
+from frt import FRT_COLUMNS, frt_table, golden_frt, match_rows
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-9
+
+
+def rel_l2(a, b):
+    a = np.asarray(a, dtype=np.float64).ravel()
+    b = np.asarray(b, dtype=np.float64).ravel()
+    den = np.linalg.norm(b)
+    return np.linalg.norm(a - b) / den if den > 0 else np.linalg.norm(a - b)
+
+
+def run_pair(name, nsteps, precision="fp64", use_graph=True, overrides=None):
+    from eqdyna_gb300.case import Case
+    from eqdyna_gb300.solver import GpuSolver
+    from oracle import Oracle
+    base = Case.from_fixture(golden_path(name), overrides=overrides)
+    cpu, gpu = base.clone(), base.clone()
+    o = Oracle(cpu, nthreads())
+    o.step(nsteps)
+    with GpuSolver(gpu, precision=precision, use_graph=use_graph) as s:
+        s.step(nsteps)
+        s.fetch()
+        assert abs(s.time - o.time) == 0.0
+        stats = s.stats()
+    return cpu, gpu, o, stats
+
+
+def fault_fields(case):
+    fr = case.fric()
+    return {"slip": fr[:, [70, 71]], "slip_rate": fr[:, [73, 74]], "peak_rate": fr[:, 75],
+            "traction": fr[:, [77, 78, 79]], "fnft": case.arrays["fnft"][: case.npair]}
+
+
+def check_parity(cpu, gpu, dt, tol=TOL, skip=()):
+    fc, fg = fault_fields(cpu), fault_fields(gpu)
+    report = {}
+    for k in ("slip", "peak_rate", "traction"):
+        if k not in skip:
+            report[k] = rel_l2(fg[k], fc[k])
+    if "slip_rate" not in skip:
+        # after arrest the final slip rate is round-off (~1e-15 m/s); measure its error against
+        # the field's dynamic range (the peak slip rate reached at each node)
+        scale = max(np.linalg.norm(fc["slip_rate"]), np.linalg.norm(fc["peak_rate"]))
+        report["slip_rate"] = np.linalg.norm(fg["slip_rate"] - fc["slip_rate"]) / scale
+    # physical-domain wavefield (3-DOF nodes, non-PML elements) at the relative bar
+    phys = cpu.arrays["numOfDofPerNodeArr"] == 3
+    vc, vg = cpu.arrays["velArr"].reshape(-1, 3), gpu.arrays["velArr"].reshape(-1, 3)
+    dc, dg = cpu.arrays["dispArr"].reshape(-1, 3), gpu.arrays["dispArr"].reshape(-1, 3)
+    report["velArr"] = rel_l2(vg[phys], vc[phys])
+    report["dispArr"] = rel_l2(dg[phys], dc[phys])
+    et = cpu.arrays["elemTypeArr"]
+    base = cpu.arrays["stressCompIndexArr"][et != 2]
+    idx = (base[:, None] + np.arange(6)[None, :]).ravel()
+    report["stressArr"] = rel_l2(gpu.arrays["stressArr"][idx], cpu.arrays["stressArr"][idx])
+    # PML nodes: absolute bound relative to the peak velocity.  On meshes sheared by an inserted
+    # dipping interface (tpv10) the reference PML carries a slowly growing mode seeded by
+    # round-off, so its nodes are not held to the relative bar.
+    pml_abs = np.abs(vg[~phys] - vc[~phys]).max() / np.abs(vc).max() if (~phys).any() else 0.0
+    report["pml_vel_abs_over_peak"] = pml_abs
+    if cpu.arrays["OffFaultStGramSCEC"] is not None:
+        report["offfault_st"] = rel_l2(gpu.arrays["OffFaultStGramSCEC"], cpu.arrays["OffFaultStGramSCEC"])
+    if cpu.sizes["numOnFaultSt"] > 0:
+        report["onfault_st"] = rel_l2(gpu.arrays["onFaultQuantHistSCECForm"], cpu.arrays["onFaultQuantHistSCECForm"])
+    bad = {k: v for k, v in report.items() if not v <= (1e-7 if k == "pml_vel_abs_over_peak" else tol)}
+    assert not bad, f"relative L2 above {tol}: {bad} (all: {report})"
+    tr_c, tr_g = fc["fnft"], fg["fnft"]
+    assert np.array_equal(tr_c > 1e4, tr_g > 1e4)
+    both = tr_c < 1e4
+    assert np.all(np.abs(tr_c[both] - tr_g[both]) <= dt * 1.000001)
+    return report
+
+
+@pytest.mark.parametrize("name,nsteps", [("tpv8", 114), ("tpv10", 60), ("tpv104", 50),
+                                         ("tpv1053d", 40), ("meng2023a", 80), ("meng2023cb", 60)])
+def test_fp64_gpu_matches_oracle(name, nsteps):
+    cpu, gpu, o, stats = run_pair(name, nsteps)
+    check_parity(cpu, gpu, cpu.scalars.dt)
+    if cpu.scalars.friclaw >= 3:
+        # the exit test is at round-off level (|r/r'| < 1e-14 |v|), so a handful of solves may
+        # stop one iteration apart
+        ref = o.stats()["newton_iters"]
+        assert abs(stats["newton_iters"] - ref) <= 1e-3 * ref
+
+
+def test_fp64_gpu_plastic_gravity_early_steps():
+    """drv.a6 (plastic, gravity, rough fault, initial stress in PML): before the round-off
+    sensitivity of its creeping region builds up (see test_oracle_golden), the GPU form agrees
+    with the oracle to 1e-9 on the wavefield, stresses and tractions; the slip-rate direction of
+    creeping nodes is round-off and is not compared."""
+    cpu, gpu, _, _ = run_pair("drv.a6", 6)
+    check_parity(cpu, gpu, cpu.scalars.dt, skip=("slip", "slip_rate", "peak_rate"))
+    assert rel_l2(gpu.arrays["pstrain"], cpu.arrays["pstrain"]) <= TOL or cpu.arrays["pstrain"].max() == 0
+
+
+def test_graph_and_stream_paths_agree():
+    _, g1, _, _ = run_pair("tpv8", 40, use_graph=True)
+    _, g2, _, _ = run_pair("tpv8", 40, use_graph=False)
+    assert rel_l2(g1.arrays["velArr"], g2.arrays["velArr"]) <= 1e-11
+
+
+def test_fp64_gpu_reproduces_reference_golden_tpv8():
+    """End to end against the reference's own output: the GPU run of test.tpv8 must print the
+    same frt.txt values (to 0.75 unit of the 7th digit) as the reference MPI build."""
+    from eqdyna_gb300.case import Case
+    from eqdyna_gb300.solver import GpuSolver
+    case = Case.from_fixture(golden_path("tpv8"))
+    with GpuSolver(case) as s:
+        s.run()
+        s.fetch()
+    ours = frt_table(case)
+    gold, _ = match_rows(ours, golden_frt(golden_path("tpv8")))
+    a = np.abs(gold)
+    e = np.where(a > 0, np.floor(np.log10(np.where(a > 0, a, 1.0))) + 1, -300)
+    tol = np.maximum(1e-3, 0.75 * 10.0 ** (e - 7))
+    bad = np.abs(ours - gold) > tol
+    j = FRT_COLUMNS.index("trup")
+    bad[:, j] &= np.abs(ours[:, j] - gold[:, j]) > case.scalars.dt
+    assert not bad.any(), {FRT_COLUMNS[k]: int(bad[:, k].sum()) for k in range(22) if bad[:, k].any()}
+
+
+def test_restart_midway_matches_continuous_run():
+    """fetch -> re-init from the fetched Fortran arrays -> continue equals an uninterrupted run
+    (the device state round-trips through the Fortran layout)."""
+    from eqdyna_gb300.case import Case
+    from eqdyna_gb300.solver import GpuSolver
+    base = Case.from_fixture(golden_path("tpv104"))
+    a, b = base.clone(), base.clone()
+    with GpuSolver(a) as s:
+        s.step(30)
+        s.fetch()
+    with GpuSolver(a) as s:
+        s.nt = 30
+        s.step(20)
+        s.fetch()
+    with GpuSolver(b) as s:
+        s.step(50)
+        s.fetch()
+    assert rel_l2(a.arrays["velArr"], b.arrays["velArr"]) <= 1e-9
+    assert rel_l2(a.fric()[:, 73], b.fric()[:, 73]) <= 1e-9
