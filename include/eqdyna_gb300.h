@@ -170,6 +170,43 @@ int eqd_gpu_kernel_time(eqd_context *ctx, int32_t kind, double *ms, int64_t *lau
  * from a register-resident FMA chain kernel; used as the compute roofline of the FP64 form. */
 int eqd_gpu_fp64_fma_peak(int32_t device, double *tflops);
 
+/* ---- element force pass without device allocation ------------------------------------------
+ * No counterpart in the reference: an addition for callers that cannot call cudaMalloc, e.g. a
+ * Fortran program whose globalvar arrays already live on the GPU under OpenACC or CUDA Fortran
+ * data management, or a host program that plans all device memory at start-up and forbids
+ * allocation during the run.  Every pointer in the view is a DEVICE pointer to the Fortran array
+ * named (same layout and 1-based index values as eqd_host_arrays). */
+typedef struct eqd_elem_device_view {
+  int32_t nnode, nelem;
+  const int32_t *nodeElemIdRelation;  /* (8, nelem)                                              */
+  const int32_t *elemTypeArr;         /* (nelem): only types 1, 11, 12, 13 are processed         */
+  const double *eleshp;               /* (3, 8, nelem)                                           */
+  const double *eledet;               /* (nelem)                                                  */
+  const double *mat;                  /* (nelem, 5)                                               */
+  const double *ss;                   /* (6, nelem)                                               */
+  const double *phi;                  /* (8, 4, nelem)                                            */
+  double *stressArr;                  /* stress(1..6) at stressCompIndexArr offsets, updated      */
+  const int32_t *stressCompIndexArr;  /* (nelem)                                                  */
+  const double *velArr, *dispArr;     /* (3, nnode)                                               */
+  double dt, rdampk, w;               /* rdampk already multiplied by dt; w = 8                   */
+} eqd_elem_device_view;
+
+/* Maximum nnode accepted by eqd_gpu_elem_forces_noalloc (size of its fixed scratch). */
+#define EQD_NOALLOC_MAX_NODES 524288
+
+/* Elastic interior-element pass of one step (calcElemKU stress update and forces plus the
+ * Kosloff-Frazier hourglass forces, binary64) on the caller's device arrays: updates stressArr in
+ * place and overwrites force_out, a DEVICE array (3, nnode), with the per-node sum of the element
+ * and hourglass forces.  PML elements (type 2) contribute nothing.  Allocates no device memory:
+ * the per-node accumulator is a fixed static device array of EQD_NOALLOC_MAX_NODES nodes
+ * (12 MiB, held by every GPU that loads the library until exit); larger meshes are rejected with
+ * EQD_ERR_INPUT.  Work is queued on `stream` (a cudaStream_t, NULL = legacy default stream) and
+ * the call returns without waiting.  The first call on a device looks up the accumulator's device
+ * address with that device current; make that first call before any stream capture.  All calls
+ * on a device share the accumulator (it is cleared at the start of each call), so calls whose
+ * work overlaps on the GPU race; serialise them on one stream. */
+int eqd_gpu_elem_forces_noalloc(const eqd_elem_device_view *view, double *force_out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
