@@ -11,7 +11,8 @@ writes, see eqdyna_gb300.case), seeded with 20261203 + config id.
   C1  rate-and-state aging law on the same box at dx = 100 m with a 4 km PML (40 layers,
       380 x 280 x 190 = 20,216,000 elements), a in [0.008, 0.016] rising smoothly outside a
       velocity-weakening core (b = 0.012), L 0.02 m, V0 1e-6 m/s, f0 0.6, initial V 1e-12 m/s,
-      241 x 121 fault node pairs, smooth overstress nucleation (TPV104 form), dt 0.004 s,
+      241 x 121 fault node pairs, sigma_n -100 MPa, tau0 60 MPa, smooth 25 MPa overstress
+      nucleation of radius 3 km at (0, -7.5 km) (TPV104 form), dt 0.004 s,
       4000 steps.
   C3  30-degree dipping reverse fault reaching the surface, degenerated wedge elements along
       the fault, slip law, depth-dependent sigma_n (16.2 MPa/km, capped at 120 MPa),
@@ -125,7 +126,7 @@ def config_c1(path, scale=1.0, nsteps=4000, npml=None):
     p = _base_params()
     dx = 100.0 * scale
     p.update(dx=dx, dy=dx, dz=dx, dt=0.004 * scale, friclaw=3, tpv=104, C_nuclea=1,
-             xsource=0.0, ysource=0.0, zsource=-7.5e3, nucR=3.0e3, nucdtau0=45.0e6, nucT=1.0)
+             xsource=0.0, ysource=0.0, zsource=-7.5e3, nucR=3.0e3, nucdtau0=25.0e6, nucT=1.0)
     p["term"] = nsteps * p["dt"]
     npml = npml if npml is not None else max(2, int(round(4000.0 / dx)))
     rng = np.random.default_rng(SEED0 + 1)

@@ -10,9 +10,13 @@
 #include "eqd_device.cuh"
 #include "mlp_common.cuh"
 
+#include <algorithm>
+#include <tuple>
+
 namespace eqd {
 ElemConst make_elem_const(const Context &c);
-int upload_fp32_tables(Context &c);
+int tile_size_interior();
+int tile_size_pml();
 }  // namespace eqd
 
 using namespace eqd;
@@ -104,6 +108,93 @@ void q_constants(double Q, int k, double &tau, double &wk, double &c1) {
   const double r = std::pow(ak0 * ak0 + bk0 * bk0, -0.5);
   c1 = 0.5 * r * (1.0 + ak0 * r);
 }
+
+// Spatially compact order of an element group for the binary32 tiles: elements are binned in
+// bricks of bx x bz x by cells (cell = median element extent of the group) and ordered brick by
+// brick, x-major, then z, then y inside a brick.  Works for any mesh; structured meshes give
+// exact bricks.
+void brick_order(const eqd_host_arrays &a, std::vector<int> &ids, int bx, int bz, int by) {
+  const size_t m = ids.size();
+  if (m == 0) return;
+  std::vector<double> c(3 * m), ext(3 * m);
+  double lo[3] = {1e300, 1e300, 1e300};
+  for (size_t i = 0; i < m; ++i) {
+    double mn[3] = {1e300, 1e300, 1e300}, mx[3] = {-1e300, -1e300, -1e300}, sum[3] = {0, 0, 0};
+    for (int q = 0; q < 8; ++q) {
+      const double *x = a.meshCoor + 3 * (size_t)(a.nodeElemIdRelation[8 * (size_t)ids[i] + q] - 1);
+      for (int k = 0; k < 3; ++k) {
+        mn[k] = std::min(mn[k], x[k]);
+        mx[k] = std::max(mx[k], x[k]);
+        sum[k] += x[k];
+      }
+    }
+    for (int k = 0; k < 3; ++k) {
+      c[3 * i + k] = sum[k] / 8.0;
+      ext[3 * i + k] = mx[k] - mn[k];
+      lo[k] = std::min(lo[k], c[3 * i + k]);
+    }
+  }
+  double h[3];
+  for (int k = 0; k < 3; ++k) {
+    std::vector<double> e(m);
+    for (size_t i = 0; i < m; ++i) e[i] = ext[3 * i + k];
+    std::nth_element(e.begin(), e.begin() + m / 2, e.end());
+    h[k] = e[m / 2] > 0 ? e[m / 2] : 1.0;
+  }
+  using Key = std::tuple<long, long, long, long, long, long, int>;
+  std::vector<Key> keys(m);
+  for (size_t i = 0; i < m; ++i) {
+    const long fx = (long)std::floor((c[3 * i] - lo[0]) / h[0] + 0.5);
+    const long fy = (long)std::floor((c[3 * i + 1] - lo[1]) / h[1] + 0.5);
+    const long fz = (long)std::floor((c[3 * i + 2] - lo[2]) / h[2] + 0.5);
+    keys[i] = Key(fx / bx, fz / bz, fy / by, fx, fz, fy, ids[i]);
+  }
+  std::sort(keys.begin(), keys.end());
+  for (size_t i = 0; i < m; ++i) ids[i] = std::get<6>(keys[i]);
+}
+
+// Tile metadata: per tile its distinct nodes (sorted device ids) and, per node, the incidences
+// (corner * tile + local element) in ascending order.
+int build_tiles(Context &c, ElemGroup<float> &g, const std::vector<int> &conn_dev, int tile) {
+  const int m = g.ne;
+  g.tile = tile;
+  g.ntiles = (m + tile - 1) / tile;
+  std::vector<int> node_ptr(1, 0), nodes, incp_off(1, 0);
+  std::vector<unsigned short> incp, inc((size_t)g.ntiles * tile * 8, 0);
+  std::vector<std::pair<int, int>> pairs;
+  int maxM = 0;
+  for (int t = 0; t < g.ntiles; ++t) {
+    const int e0 = t * tile, e1 = std::min(m, e0 + tile);
+    pairs.clear();
+    for (int e = e0; e < e1; ++e)
+      for (int q = 0; q < 8; ++q) pairs.push_back({conn_dev[(size_t)q * m + e], q * tile + (e - e0)});
+    std::sort(pairs.begin(), pairs.end());
+    int M = 0;
+    const size_t base = (size_t)t * tile * 8;
+    for (size_t k = 0; k < pairs.size(); ++k) {
+      if (k == 0 || pairs[k].first != pairs[k - 1].first) {
+        nodes.push_back(pairs[k].first);
+        incp.push_back((unsigned short)k);
+        ++M;
+      }
+      inc[base + k] = (unsigned short)pairs[k].second;
+    }
+    incp.push_back((unsigned short)pairs.size());
+    node_ptr.push_back((int)nodes.size());
+    incp_off.push_back((int)incp.size());
+    maxM = std::max(maxM, M);
+  }
+  g.max_tile_nodes = std::max(maxM, 1);
+  int rc;
+  if ((rc = dupload(c, g.tile_node_ptr, node_ptr))) return rc;
+  if ((rc = dupload(c, g.tile_nodes, nodes))) return rc;
+  if ((rc = dupload(c, g.tile_incp, incp))) return rc;
+  if ((rc = dupload(c, g.tile_incp_off, incp_off))) return rc;
+  if ((rc = dupload(c, g.tile_inc, inc))) return rc;
+  return EQD_OK;
+}
+
+std::vector<float> to_f32(const std::vector<double> &v) { return std::vector<float>(v.begin(), v.end()); }
 
 int validate(const eqd_scalars *s, const eqd_host_arrays *a) {
   if (!s || !a) return EQD_ERR_INPUT;
@@ -199,12 +290,39 @@ int build_device_state(eqd_context &X, const eqd_scalars &s, const eqd_host_arra
   }
   RC(dupload(c, c.vel, vel));
   RC(dupload(c, c.disp, disp));
-  RC(dupload(c, c.F, F));
   RC(dupload(c, c.inv_mass, inv_mass));
-  RC(dupload(c, c.F9, F9));
-  RC(dupload(c, c.v9, v9));
   RC(dupload(c, c.vh, vh));
-  RC(dupload(c, c.pml_ab, pml_ab));
+  if (c.fp32) {
+    // binary32 form: force sums, PML split velocities, damping and 1/m in binary32
+    RC(dupload(c, c.F32, to_f32(F)));
+    RC(dupload(c, c.F9_32, to_f32(F9)));
+    RC(dupload(c, c.v9_32, to_f32(v9)));
+    RC(dupload(c, c.pml_ab32, to_f32(pml_ab)));
+    // split (fault) nodes keep binary64 forces and updates: mark them with a negative 1/m and
+    // give each a slot (2 i slave, 2 i + 1 master of pair i) in the binary64 force array
+    std::vector<float> im32 = to_f32(inv_mass);
+    const int npair0 = (a.ntotft >= 1 && a.nftnd) ? a.nftnd[0] : 0;
+    std::vector<int> slot(nn, -1);
+    std::vector<double> fsplit(3 * (size_t)std::max(2 * npair0, 1), 0.0);
+    for (int i = 0; i < npair0; ++i)
+      for (int k = 0; k < 2; ++k) {
+        const int node = a.nsmp[2 * (size_t)i + k];
+        if (node < 1 || node > nn) return EQD_ERR_INPUT;
+        const int d = X.node_dev[node - 1];
+        if (d >= c.n_int) return EQD_ERR_UNSUPPORTED;
+        slot[d] = 2 * i + k;
+        im32[d] = -im32[d];
+        for (int q = 0; q < 3; ++q) fsplit[(size_t)q * 2 * npair0 + 2 * i + k] = F[(size_t)q * nn + d];
+      }
+    RC(dupload(c, c.inv_mass32, im32));
+    RC(dupload(c, c.split_slot, slot));
+    RC(dupload(c, c.Fsplit, fsplit));
+  } else {
+    RC(dupload(c, c.F, F));
+    RC(dupload(c, c.F9, F9));
+    RC(dupload(c, c.v9, v9));
+    RC(dupload(c, c.pml_ab, pml_ab));
+  }
   c.f_is_acc = 1;
 
   // ---- elements ----
@@ -217,11 +335,17 @@ int build_device_state(eqd_context &X, const eqd_scalars &s, const eqd_host_arra
     else return EQD_ERR_INPUT;
   }
   const bool body = (s.rdampm != 0.0) || (s.C_elastic == 0);
+  if (c.fp32) {
+    if (s.C_Q == 1) return EQD_ERR_UNSUPPORTED;  // Q memory variables: binary64 form only
+    brick_order(a, X.gi_orig, 4, 4, 8);
+    brick_order(a, X.gp_orig, 4, 4, 8);
+  }
   for (int grp = 0; grp < 2; ++grp) {
     const std::vector<int> &ids = grp == 0 ? X.gi_orig : X.gp_orig;
     ElemGroup<double> &g = grp == 0 ? c.gi64 : c.gp64;
     const int m = (int)ids.size();
-    g.ne = m;
+    if (!c.fp32) g.ne = m;
+    else (grp == 0 ? c.gi32 : c.gp32).ne = m;
     if (m == 0) continue;
     std::vector<int> conn(8 * (size_t)m);
     std::vector<double> shp(24 * (size_t)m), phi(32 * (size_t)m), ss(6 * (size_t)m), detw(m), lam(m), mu(m);
@@ -297,6 +421,24 @@ int build_device_state(eqd_context &X, const eqd_scalars &s, const eqd_host_arra
         qc[4 * (size_t)m + i] = wks * 8.0;
       }
     }
+    if (c.fp32) {
+      ElemGroup<float> &h = grp == 0 ? c.gi32 : c.gp32;
+      RC(build_tiles(c, h, conn, grp == 0 ? tile_size_interior() : tile_size_pml()));
+      RC(dupload(c, h.shp, to_f32(shp)));
+      RC(dupload(c, h.phi, to_f32(phi)));
+      RC(dupload(c, h.ss, to_f32(ss)));
+      RC(dupload(c, h.detw, to_f32(detw)));
+      RC(dupload(c, h.lam, to_f32(lam)));
+      RC(dupload(c, h.mu, to_f32(mu)));
+      RC(dupload(c, h.stress, to_f32(st)));
+      if (grp == 1 && any_s0) RC(dupload(c, h.stress0, to_f32(st0)));
+      if (grp == 1) RC(dupload(c, h.pml_ab, to_f32(pab)));
+      if (body) RC(dupload(c, h.em, to_f32(em)));
+      if (s.C_hg == 2) RC(dupload(c, h.hgcoef, to_f32(hg)));
+      if (!porep.empty()) RC(dupload(c, h.porep, to_f32(porep)));
+      if (!pstr.empty()) RC(dupload(c, h.pstrain, pstr));
+      continue;
+    }
     RC(dupload(c, g.conn, conn));
     RC(dupload(c, g.shp, shp));
     RC(dupload(c, g.phi, phi));
@@ -312,6 +454,12 @@ int build_device_state(eqd_context &X, const eqd_scalars &s, const eqd_host_arra
     if (!porep.empty()) RC(dupload(c, g.porep, porep));
     if (!pstr.empty()) RC(dupload(c, g.pstrain, pstr));
     if (!qc.empty()) RC(dupload(c, g.qcoef, qc));
+  }
+  if (c.fp32) {
+    RC(dalloc(c, c.vel32, 3 * (size_t)nn));
+    RC(dalloc(c, c.dl32, 3 * (size_t)nn));
+    EQD_CUDA_OK(cudaMemset(c.vel32, 0, 3 * (size_t)nn * sizeof(float)));
+    EQD_CUDA_OK(cudaMemset(c.dl32, 0, 3 * (size_t)nn * sizeof(float)));
   }
 
   // ---- fault ----
@@ -560,7 +708,6 @@ int eqd_gpu_init(const eqd_scalars *s, const eqd_host_arrays *a, const eqd_optio
   }
   c.fp32 = (c.opt.precision == EQD_PREC_FP32);
   rc = build_device_state(*X, *s, *a);
-  if (!rc && c.fp32) rc = upload_fp32_tables(c);
   if (!rc && c.opt.learned_guess) rc = mlp_init(c);
   if (!rc && cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking) != cudaSuccess) rc = EQD_ERR_CUDA;
   if (rc) {
@@ -650,12 +797,39 @@ int eqd_gpu_fetch(eqd_context *X, eqd_host_arrays *a) {
   std::vector<double> v9(9 * (size_t)np_), vh(3 * (size_t)np_), F9(9 * (size_t)np_);
   EQD_CUDA_OK(cudaMemcpy(vel.data(), c.vel, vel.size() * 8, cudaMemcpyDeviceToHost));
   EQD_CUDA_OK(cudaMemcpy(disp.data(), c.disp, disp.size() * 8, cudaMemcpyDeviceToHost));
-  EQD_CUDA_OK(cudaMemcpy(F.data(), c.F, F.size() * 8, cudaMemcpyDeviceToHost));
   EQD_CUDA_OK(cudaMemcpy(im.data(), c.inv_mass, im.size() * 8, cudaMemcpyDeviceToHost));
+  auto get32 = [&](std::vector<double> &dst, const float *src) -> int {
+    std::vector<float> t(dst.size());
+    if (!t.empty() && cudaMemcpy(t.data(), src, t.size() * 4, cudaMemcpyDeviceToHost) != cudaSuccess) return EQD_ERR_CUDA;
+    for (size_t q = 0; q < t.size(); ++q) dst[q] = t[q];
+    return EQD_OK;
+  };
+  if (c.fp32) {
+    RC(get32(F, c.F32));
+    if (c.npair > 0) {
+      std::vector<double> fs(3 * (size_t)2 * c.npair);
+      std::vector<int> ps(c.npair), pm(c.npair);
+      EQD_CUDA_OK(cudaMemcpy(fs.data(), c.Fsplit, fs.size() * 8, cudaMemcpyDeviceToHost));
+      EQD_CUDA_OK(cudaMemcpy(ps.data(), c.pair_s, ps.size() * 4, cudaMemcpyDeviceToHost));
+      EQD_CUDA_OK(cudaMemcpy(pm.data(), c.pair_m, pm.size() * 4, cudaMemcpyDeviceToHost));
+      for (int i = 0; i < c.npair; ++i)
+        for (int q = 0; q < 3; ++q) {
+          F[(size_t)q * nn + ps[i]] = fs[(size_t)q * 2 * c.npair + 2 * i];
+          F[(size_t)q * nn + pm[i]] = fs[(size_t)q * 2 * c.npair + 2 * i + 1];
+        }
+    }
+  } else {
+    EQD_CUDA_OK(cudaMemcpy(F.data(), c.F, F.size() * 8, cudaMemcpyDeviceToHost));
+  }
   if (np_ > 0) {
-    EQD_CUDA_OK(cudaMemcpy(v9.data(), c.v9, v9.size() * 8, cudaMemcpyDeviceToHost));
     EQD_CUDA_OK(cudaMemcpy(vh.data(), c.vh, vh.size() * 8, cudaMemcpyDeviceToHost));
-    EQD_CUDA_OK(cudaMemcpy(F9.data(), c.F9, F9.size() * 8, cudaMemcpyDeviceToHost));
+    if (c.fp32) {
+      RC(get32(v9, c.v9_32));
+      RC(get32(F9, c.F9_32));
+    } else {
+      EQD_CUDA_OK(cudaMemcpy(v9.data(), c.v9, v9.size() * 8, cudaMemcpyDeviceToHost));
+      EQD_CUDA_OK(cudaMemcpy(F9.data(), c.F9, F9.size() * 8, cudaMemcpyDeviceToHost));
+    }
   }
   auto eq = [&](int j, int k) { return a->eqNumIndexArr[a->eqNumStartIndexLoc[j] + k - 1]; };
   for (int d = 0; d < nn; ++d) {
@@ -705,10 +879,12 @@ int eqd_gpu_fetch(eqd_context *X, eqd_host_arrays *a) {
       }
     }
   }
-  if (a->pstrain && c.gi64.pstrain) {
-    std::vector<double> ps(c.gi64.ne);
-    EQD_CUDA_OK(cudaMemcpy(ps.data(), c.gi64.pstrain, ps.size() * 8, cudaMemcpyDeviceToHost));
-    for (int i = 0; i < c.gi64.ne; ++i) a->pstrain[X->gi_orig[i]] = ps[i];
+  const double *dps = c.fp32 ? c.gi32.pstrain : c.gi64.pstrain;
+  const int nps = c.fp32 ? c.gi32.ne : c.gi64.ne;
+  if (a->pstrain && dps) {
+    std::vector<double> ps(nps);
+    EQD_CUDA_OK(cudaMemcpy(ps.data(), dps, ps.size() * 8, cudaMemcpyDeviceToHost));
+    for (int i = 0; i < nps; ++i) a->pstrain[X->gi_orig[i]] = ps[i];
   }
   RC(eqd_gpu_fetch_fault(X, a->fric, a->fnft));
   if (c.nstep > 0) {

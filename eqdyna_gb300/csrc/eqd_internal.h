@@ -41,6 +41,15 @@ struct ElemGroup {
   T *porep = nullptr;        // [ne]
   T *qcoef = nullptr;        // Q: [5][ne]  exp(-dt/tau), miuu, Mu, wkp, wks
   int *orig = nullptr;       // [ne] original element id (0-based)
+  // tiles (binary32 form): consecutive runs of `tile` elements of a spatially compact brick
+  // order; each tile lists its distinct nodes and, per node, the (element, corner) incidences
+  int tile = 0, ntiles = 0, max_tile_nodes = 0;
+  int ld = 0;                       // SoA stride of the binary32 tables: ntiles * tile (padded)
+  int *tile_node_ptr = nullptr;     // [ntiles + 1] offsets into tile_nodes
+  int *tile_nodes = nullptr;        // device node ids, sorted, per tile
+  unsigned short *tile_incp = nullptr;  // per tile: M + 1 offsets into that tile's incidences
+  int *tile_incp_off = nullptr;     // [ntiles + 1] offsets into tile_incp
+  unsigned short *tile_inc = nullptr;   // [ntiles * tile * 8] incidences (e_local * 8 + corner)
 };
 
 struct PairStation {
@@ -59,8 +68,13 @@ struct Context {
   // node state
   double *vel = nullptr, *disp = nullptr, *F = nullptr, *inv_mass = nullptr;
   double *F9 = nullptr, *v9 = nullptr, *vh = nullptr, *pml_ab = nullptr;
-  float *F32 = nullptr;          // FP32 form: compensated force accumulator [2][3][nnode]
-  float *F9_32 = nullptr;        // FP32 form: [2][9][npml]
+  float *F32 = nullptr;          // FP32 form: force accumulator [3][nnode] (replaces F)
+  float *F9_32 = nullptr;        // FP32 form: split-field force accumulator [9][npml] (replaces F9)
+  float *v9_32 = nullptr;        // FP32 form: PML split-field velocities [9][npml] (replaces v9)
+  float *pml_ab32 = nullptr;     // FP32 form: [6][npml] node damping coefficients
+  float *inv_mass32 = nullptr;   // FP32 form: [nnode]; negative marks a split (fault) node
+  double *Fsplit = nullptr;      // FP32 form: binary64 forces of split nodes [3][2 * npair]
+  int *split_slot = nullptr;     // FP32 form: [nnode] slot of a split node in Fsplit
   float *vel32 = nullptr;        // FP32 form: [3][nnode] velocity copy
   float *dl32 = nullptr;         // FP32 form: [3][nnode] disp + rdampk * vel copy
   int *node_orig = nullptr;      // host only: device id -> original node id (0-based)

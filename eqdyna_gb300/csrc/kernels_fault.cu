@@ -17,13 +17,16 @@ namespace {
 constexpr int kBlockNode = 256;
 constexpr int kBlockFault = 128;
 
-template <bool F_IS_ACC>
+// COPY32: also writes the binary32 copies of velocity and of u + rdampk v read by the binary32
+// element kernels (the binary64 arrays stay the state).
+template <bool F_IS_ACC, bool COPY32>
 __global__ void __launch_bounds__(kBlockNode)
     node_update(double *__restrict__ vel, double *__restrict__ disp, double *__restrict__ F,
                 const double *__restrict__ inv_mass, double *__restrict__ F9,
                 double *__restrict__ v9, double *__restrict__ vh,
                 const double *__restrict__ pml_ab, int nnode, int n_int, int npml, double dt,
-                int *__restrict__ d_nt, int *__restrict__ d_err) {
+                int *__restrict__ d_nt, int *__restrict__ d_err, float *__restrict__ vel32,
+                float *__restrict__ dl32, double rdampk) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i == 0) *d_nt += 1;
   if (i >= nnode) return;
@@ -76,6 +79,106 @@ __global__ void __launch_bounds__(kBlockNode)
       }
     }
   }
+  if (COPY32) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      vel32[c * nnode + i] = (float)v[c];
+      dl32[c * nnode + i] = (float)fma(rdampk, v[c], disp[c * nnode + i]);
+    }
+  }
+  if (isnan(v[0]) || isnan(v[1]) || isnan(v[2])) atomicOr(d_err, 1);
+}
+
+// Node update of the binary32 form.  The force sums arrive in binary32 (Kahan-compensated per
+// tile); acceleration, its increment a*dt and the PML split-field velocities are binary32, while
+// velocity and displacement of every node stay binary64 (increments are small against the state,
+// which is accumulated over 10^3 - 10^4 steps).  About 6 binary64 operations per component.
+template <bool F_IS_ACC>
+__global__ void __launch_bounds__(kBlockNode)
+    node_update32(double *__restrict__ vel, double *__restrict__ disp, float *__restrict__ F,
+                  const float *__restrict__ inv_mass, float *__restrict__ F9,
+                  float *__restrict__ v9, double *__restrict__ vh,
+                  const float *__restrict__ pml_ab, int nnode, int n_int, int npml, float dt,
+                  double dtd, int *__restrict__ d_nt, int *__restrict__ d_err,
+                  float *__restrict__ vel32, float *__restrict__ dl32, double rdampk,
+                  const double *__restrict__ Fsplit, const int *__restrict__ split_slot, int nsplit) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i == 0) *d_nt += 1;
+  if (i >= nnode) return;
+  const float im = inv_mass[i];
+  double v[3];
+  if (im < 0.f) {
+    // split (fault) node: the fault kernel set its force in binary64; update it in binary64 so
+    // the slave-master relative motion keeps binary64 resolution (creep rates ~1e-12..1e-16 m/s)
+    const int q = split_slot[i];
+    const double imd = -(double)im;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const double f = Fsplit[(size_t)c * nsplit + q];
+      const double acc = F_IS_ACC ? f : f * imd;
+      v[c] = fma(acc, dtd, vel[c * nnode + i]);
+      vel[c * nnode + i] = v[c];
+      const double u = fma(v[c], dtd, disp[c * nnode + i]);
+      disp[c * nnode + i] = u;
+      F[c * nnode + i] = 0.f;
+      vel32[c * nnode + i] = (float)v[c];
+      dl32[c * nnode + i] = (float)fma(rdampk, v[c], u);
+    }
+  } else if (i < n_int) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const float f = F[c * nnode + i];
+      const float dv = F_IS_ACC ? f * dt : f * im * dt;
+      v[c] = vel[c * nnode + i] + (double)dv;
+      vel[c * nnode + i] = v[c];
+      const double u = fma(v[c], dtd, disp[c * nnode + i]);
+      disp[c * nnode + i] = u;
+      F[c * nnode + i] = 0.f;
+      vel32[c * nnode + i] = (float)v[c];
+      dl32[c * nnode + i] = (float)fma(rdampk, v[c], u);
+    }
+  } else {
+    const int p = i - n_int;
+    if (im == 0.f) {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        v[c] = 0.0;
+        vel[c * nnode + i] = 0.0;
+        disp[c * nnode + i] = 0.0;
+        F[c * nnode + i] = 0.f;
+        vel32[c * nnode + i] = 0.f;
+        dl32[c * nnode + i] = 0.f;
+      }
+#pragma unroll
+      for (int j = 0; j < 9; ++j) F9[j * npml + p] = 0.f;
+    } else {
+      float vs[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+      for (int j = 0; j < 9; ++j) {
+        const int ax = j % 3;
+        const float f = F9[j * npml + p];
+        const float acc = F_IS_ACC ? f : f * im;
+        const float nv = fmaf(pml_ab[ax * npml + p], v9[j * npml + p], acc) * pml_ab[(3 + ax) * npml + p];
+        v9[j * npml + p] = nv;
+        vs[j / 3] += nv;
+        F9[j * npml + p] = 0.f;
+      }
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const float f = F[c * nnode + i];
+        const float dv = F_IS_ACC ? f * dt : f * im * dt;
+        const double nh = vh[c * npml + p] + (double)dv;
+        vh[c * npml + p] = nh;
+        v[c] = (double)vs[c] + nh;
+        vel[c * nnode + i] = v[c];
+        const double u = fma(v[c], dtd, disp[c * nnode + i]);
+        disp[c * nnode + i] = u;
+        F[c * nnode + i] = 0.f;
+        vel32[c * nnode + i] = (float)v[c];
+        dl32[c * nnode + i] = (float)fma(rdampk, v[c], u);
+      }
+    }
+  }
   if (isnan(v[0]) || isnan(v[1]) || isnan(v[2])) atomicOr(d_err, 1);
 }
 
@@ -92,7 +195,9 @@ struct FaultArgs {
   double *onhist;
   const int *off_rows;
   double *offhist;
-  double *F;
+  double *F;                  // binary64 form forces, or null
+  float *F32;                 // binary32 form element-force sums, or null
+  double *Fsplit;             // binary32 form: binary64 output forces [3][2 * npair]
   const double *vel, *disp;
   const int *d_nt;
   const double *d_times;
@@ -127,6 +232,20 @@ __device__ __forceinline__ void rsf_law(int friclaw, double V2, double &state, c
 #undef FR
 }
 
+// Force of node `node`, component c, in the form's own precision.
+template <bool F32>
+__device__ __forceinline__ double force_get(const FaultArgs &p, int c, int node) {
+  return F32 ? (double)p.F32[(size_t)c * p.nnode + node] : p.F[(size_t)c * p.nnode + node];
+}
+// Writes the pair's new force.  The binary32 form keeps split-node forces in binary64 (slot
+// 2 i for the slave, 2 i + 1 for the master of pair i).
+template <bool F32>
+__device__ __forceinline__ void force_set(const FaultArgs &p, int c, int node, int slot, double v) {
+  if (F32) p.Fsplit[(size_t)c * 2 * p.npair + slot] = v;
+  else p.F[(size_t)c * p.nnode + node] = v;
+}
+
+template <bool F32>
 __global__ void __launch_bounds__(kBlockFault) fault_kernel(FaultArgs p) {
   const int nt = *p.d_nt;
   const double t = p.d_times[nt];
@@ -187,7 +306,7 @@ __global__ void __launch_bounds__(kBlockFault) fault_kernel(FaultArgs p) {
     double x[3][3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-      x[0][c] = p.F[c * nn + node];
+      x[0][c] = force_get<F32>(p, c, node);
       x[1][c] = p.vel[c * nn + node];
       x[2][c] = p.disp[c * nn + node];
     }
@@ -240,7 +359,6 @@ __global__ void __launch_bounds__(kBlockFault) fault_kernel(FaultArgs p) {
   }
   tr[3] = sqrt(tr[1] * tr[1] + tr[2] * tr[2]);
 
-  double *Fs = p.F + sl, *Fm = p.F + ms;
   unsigned iters = 0, maxhit = 0;
   if (p.friclaw <= 2) {
     // solveSWTW (src/faulting.f90:136-188)
@@ -279,8 +397,8 @@ __global__ void __launch_bounds__(kBlockFault) fault_kernel(FaultArgs p) {
     for (int j = 0; j < 3; ++j) {
       const double xt = (tr[0] * un[j] + tr[1] * us[j] + tr[2] * ud[j]) * arn;
       const double xi = (init[0] * un[j] + init[1] * us[j] + init[2] * ud[j]) * arn;
-      Fs[j * nn] = Fs[j * nn] + xt - xi * p.C_elastic;
-      Fm[j * nn] = Fm[j * nn] - xt + xi * p.C_elastic;
+      force_set<F32>(p, j, sl, 2 * i, force_get<F32>(p, j, sl) + xt - xi * p.C_elastic);
+      force_set<F32>(p, j, ms, 2 * i + 1, force_get<F32>(p, j, ms) - xt + xi * p.C_elastic);
     }
     FR(78) = tr[0];
     FR(79) = tr[1];
@@ -373,9 +491,9 @@ __global__ void __launch_bounds__(kBlockFault) fault_kernel(FaultArgs p) {
 #pragma unroll
     for (int j = 0; j < 3; ++j) {
       const double xa = acc[0] * un[j] + acc[1] * us[j] + acc[2] * ud[j];
-      const double R = Fs[j * nn] + Fm[j * nn];
-      Fs[j * nn] = (-xa + R / mM) * mr;
-      Fm[j * nn] = (xa + R / mS) * mr;
+      const double R = force_get<F32>(p, j, sl) + force_get<F32>(p, j, ms);
+      force_set<F32>(p, j, sl, 2 * i, (-xa + R / mM) * mr);
+      force_set<F32>(p, j, ms, 2 * i + 1, (xa + R / mS) * mr);
       FR(31 + j) = p.vel[j * nn + ms] + (xa + R / mS) * dt;
       FR(34 + j) = p.vel[j * nn + sl] + (-xa + R / mM) * dt;
     }
@@ -412,14 +530,20 @@ __global__ void __launch_bounds__(kBlockFault) fault_kernel(FaultArgs p) {
 
 int launch_node_update(Context &c, cudaStream_t s) {
   const int grid = (c.nnode + kBlockNode - 1) / kBlockNode;
-  if (c.f_is_acc)
-    node_update<true><<<grid, kBlockNode, 0, s>>>(c.vel, c.disp, c.F, c.inv_mass, c.F9, c.v9, c.vh,
-                                                  c.pml_ab, c.nnode, c.n_int, c.npml, c.sc.dt,
-                                                  c.d_nt, c.d_err);
-  else
-    node_update<false><<<grid, kBlockNode, 0, s>>>(c.vel, c.disp, c.F, c.inv_mass, c.F9, c.v9, c.vh,
-                                                   c.pml_ab, c.nnode, c.n_int, c.npml, c.sc.dt,
-                                                   c.d_nt, c.d_err);
+#define EQD_NODE_ARGS c.vel, c.disp, c.F, c.inv_mass, c.F9, c.v9, c.vh, c.pml_ab, c.nnode, c.n_int, \
+    c.npml, c.sc.dt, c.d_nt, c.d_err, c.vel32, c.dl32, c.sc.rdampk
+  if (c.fp32) {
+#define EQD_NODE32_ARGS c.vel, c.disp, c.F32, c.inv_mass32, c.F9_32, c.v9_32, c.vh, c.pml_ab32, c.nnode, \
+    c.n_int, c.npml, (float)c.sc.dt, c.sc.dt, c.d_nt, c.d_err, c.vel32, c.dl32, c.sc.rdampk, c.Fsplit, \
+    c.split_slot, 2 * c.npair
+    if (c.f_is_acc) node_update32<true><<<grid, kBlockNode, 0, s>>>(EQD_NODE32_ARGS);
+    else node_update32<false><<<grid, kBlockNode, 0, s>>>(EQD_NODE32_ARGS);
+#undef EQD_NODE32_ARGS
+  } else {
+    if (c.f_is_acc) node_update<true, false><<<grid, kBlockNode, 0, s>>>(EQD_NODE_ARGS);
+    else node_update<false, false><<<grid, kBlockNode, 0, s>>>(EQD_NODE_ARGS);
+  }
+#undef EQD_NODE_ARGS
   return cudaGetLastError() == cudaSuccess ? EQD_OK : EQD_ERR_CUDA;
 }
 
@@ -455,7 +579,9 @@ int launch_fault(Context &c, cudaStream_t s) {
   p.onhist = c.onhist;
   p.off_rows = c.off_rows;
   p.offhist = c.offhist;
-  p.F = c.F;
+  p.F = c.fp32 ? nullptr : c.F;
+  p.F32 = c.fp32 ? c.F32 : nullptr;
+  p.Fsplit = c.Fsplit;
   p.vel = c.vel;
   p.disp = c.disp;
   p.d_nt = c.d_nt;
@@ -463,7 +589,8 @@ int launch_fault(Context &c, cudaStream_t s) {
   p.stats = c.d_stats;
   p.mlp = static_cast<const MlpDevice *>(mlp_device_params(c));
   const int grid = (nthreads + kBlockFault - 1) / kBlockFault;
-  fault_kernel<<<grid, kBlockFault, 0, s>>>(p);
+  if (c.fp32) fault_kernel<true><<<grid, kBlockFault, 0, s>>>(p);
+  else fault_kernel<false><<<grid, kBlockFault, 0, s>>>(p);
   return cudaGetLastError() == cudaSuccess ? EQD_OK : EQD_ERR_CUDA;
 }
 
