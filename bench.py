@@ -41,14 +41,20 @@ sys.path.insert(0, ROOT)
 METRIC = "element-updates/s, FP32+learned vs plain FP64 on 1 GB300 at ≤1% slip-rate L2 error"
 UNIT = "element-updates/s"
 
-# Algorithmic bytes per element update (compulsory traffic with per-element stored tables and
-# perfect reuse of nodal data).  Element tables: connectivity, shape gradients, det, lambda/mu,
-# stress read+write, hourglass vectors and stiffness (+ damping / split stress for PML).  Node
-# share: gather of velocity and displacement plus the force scatter.
+# Algorithmic bytes per element update: the compulsory traffic of the layout the kernel uses, with
+# perfect reuse of nodal data.
+#   fp64 (per-element tables): connectivity 32, shape gradients 192, det 8, lambda/mu 16, stress
+#     read+write 96 (PML 240), hourglass vectors 256 and stiffness 48, PML factors 48.
+#   fp32 streamed: incidence list 16 (replaces connectivity), then the fp64 tables in binary32.
+#   fp32 record-indexed: incidence list 16, record index 4, stress read+write 48 (PML 120), PML
+#     axis indices 8; plus the record table once per launch (records x floats x 4).
+# Node share: gather of velocity and displacement plus the force scatter (+ split fields on PML
+# nodes).
 ELEM_BYTES = {"fp64": {"interior": 32 + 192 + 8 + 16 + 96 + 256 + 48,
                        "pml": 32 + 192 + 8 + 16 + 240 + 256 + 48 + 48},
-              "fp32": {"interior": 32 + 96 + 4 + 8 + 48 + 128 + 24,
-                       "pml": 32 + 96 + 4 + 8 + 120 + 128 + 24 + 24}}
+              "fp32": {"interior": 16 + 96 + 4 + 8 + 48 + 128 + 24,
+                       "pml": 16 + 96 + 4 + 8 + 120 + 128 + 24 + 24}}
+REC_ELEM_BYTES = {"interior": 16 + 4 + 48, "pml": 16 + 4 + 120 + 8}
 NODE_GATHER_BYTES = {"fp64": 48 + 24, "fp32": 24 + 12}
 PML_NODE_EXTRA = {"fp64": 72, "fp32": 36}
 FP64_FLOPS_PER_ELEM = {"interior": 2 * 423, "pml": 2 * 470}
@@ -125,8 +131,9 @@ def build_case(config, scale, nsteps, workdir):
     return Case.from_dir(workdir)
 
 
-def algorithmic_bytes(case, precision):
-    """Per-launch algorithmic bytes of the two element kernels (interior, PML)."""
+def algorithmic_bytes(case, precision, tables=None):
+    """Per-launch algorithmic bytes of the two element kernels (interior, PML) for the table
+    layout each group runs with (`tables` = GpuSolver.table_info())."""
     import numpy as np
     a = case.arrays
     et = a["elemTypeArr"]
@@ -137,8 +144,12 @@ def algorithmic_bytes(case, precision):
         ne = int(mask.sum())
         nodes = np.unique(conn[mask]) - 1 if ne else np.zeros(0, dtype=np.int64)
         npml_nodes = int((nd[nodes] == 12).sum()) if ne else 0
-        out[name] = (ne * ELEM_BYTES[precision][name] + len(nodes) * NODE_GATHER_BYTES[precision]
-                     + npml_nodes * PML_NODE_EXTRA[precision], ne)
+        t = (tables or {}).get(name) or {}
+        if precision == "fp32" and t.get("layout") == "records":
+            elem = ne * REC_ELEM_BYTES[name] + t["records"] * t["record_floats"] * 4
+        else:
+            elem = ne * ELEM_BYTES[precision][name]
+        out[name] = (elem + len(nodes) * NODE_GATHER_BYTES[precision] + npml_nodes * PML_NODE_EXTRA[precision], ne)
     return out
 
 
@@ -250,7 +261,8 @@ def bench_ours(args, world, rank, local):
     fn = np.zeros_like(e2e_case.arrays["fnft"])
     barrier(world)
     t0 = time.perf_counter()
-    s = GpuSolver(e2e_case, precision=args.precision, learned_guess=args.learned, device=local)
+    s = GpuSolver(e2e_case, precision=args.precision, learned_guess=args.learned, device=local,
+                  table_layout=args.tables)
     for _ in range(args.steps):
         s.step(1)
         s.fetch_fault(fr, fn)
@@ -263,7 +275,8 @@ def bench_ours(args, world, rank, local):
     d2h_per_step = 100 * npair * 8 + npair * 8
 
     # ---- device-timed steps ----
-    s = GpuSolver(case, precision=args.precision, learned_guess=args.learned, device=local)
+    s = GpuSolver(case, precision=args.precision, learned_guess=args.learned, device=local,
+                  table_layout=args.tables)
     s.step(args.warmup)
     s.profile(True, reset=True)
     barrier(world)
@@ -275,6 +288,7 @@ def bench_ours(args, world, rank, local):
     s.profile(False)
     kt = s.kernel_times()
     stats = s.stats()
+    tables = s.table_info()
     step_ms_total = kt["step"][0]
     dev_s = allreduce_max(step_ms_total / 1e3, world)
     units = allreduce_sum(float(ne) * args.steps, world)
@@ -283,7 +297,8 @@ def bench_ours(args, world, rank, local):
 
     # ---- roofline of the dominant kernel ----
     hbm_peak, peak_kind = _peaks()
-    ab = algorithmic_bytes(case, args.precision)
+    ab = algorithmic_bytes(case, args.precision, tables)
+    working_set = ab["interior"][0] + ab["pml"][0]
     dom = "elem_interior" if kt["elem_interior"][0] >= kt["elem_pml"][0] else "elem_pml"
     key = "interior" if dom == "elem_interior" else "pml"
     ms, nl = kt[dom]
@@ -313,7 +328,9 @@ def bench_ours(args, world, rank, local):
             "config": {"workload": f"{args.config}: {WORKLOADS[args.config]}", "elements": ne,
                        "physical_elements": case.dims["n_phys_elem"], "precision": args.precision,
                        "learned_guess": bool(args.learned), "scale": args.scale,
-                       "l2": f"inputs larger than L2 (element tables alone {host_bytes_in / 1e9:.1f} GB)",
+                       "l2": f"inputs larger than L2: element-kernel working set "
+                             f"{working_set / 1e9:.2f} GB per step vs 129 MB L2, no flush",
+                       "element_tables": {k: (v["layout"], v["records"]) for k, v in tables.items()},
                        "parallelism": "replicas" if world > 1 else "single GPU",
                        "setup_s": round(setup_s, 1), "wall_ms_per_step": wall * 1e3 / args.steps},
             "e2e": {"value": units / e2e_s if world > 1 else ne * args.steps / e2e_s, "unit": UNIT,
@@ -335,8 +352,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--config", default="C1")
     ap.add_argument("--scale", type=float, default=1.0)
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
+    ap.add_argument("--precision", default="fp32", choices=["fp64", "fp32"])
     ap.add_argument("--learned", type=int, default=0)
+    ap.add_argument("--tables", default="auto", choices=["auto", "streamed", "records"],
+                    help="binary32 element-table layout")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     args = ap.parse_args()

@@ -69,11 +69,14 @@ INT_ARRAYS = {n for n, t in HOST_ARRAY_FIELDS + FAULT_FIELDS + STATION_FIELDS if
 class EqdOptions(C.Structure):
     _fields_ = [("precision", C.c_int32), ("learned_guess", C.c_int32),
                 ("record_tp_hist", C.c_int32), ("block_elem", C.c_int32),
-                ("use_graph", C.c_int32), ("device", C.c_int32), ("reserved", C.c_int32 * 2)]
+                ("use_graph", C.c_int32), ("device", C.c_int32), ("table_layout", C.c_int32),
+                ("reserved", C.c_int32)]
 
 
 PREC_FP64 = 0
 PREC_FP32 = 1
+
+TABLE_LAYOUTS = {"auto": 0, "streamed": 1, "records": 2}
 
 STATUS = {0: "ok", 1: "bad input", 2: "CUDA error", 3: "device out of memory", 4: "NaN velocity",
           5: "unsupported option", 6: "no CUDA device", 7: "bounded wait timed out",
@@ -148,6 +151,8 @@ def gpu_lib():
         lib.eqd_gpu_kernel_time.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_double),
                                             C.POINTER(C.c_int64)]
         lib.eqd_gpu_kernel_time.restype = C.c_int
+        lib.eqd_gpu_table_info.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_int64)]
+        lib.eqd_gpu_table_info.restype = C.c_int
         lib.eqd_gpu_fp64_fma_peak.argtypes = [C.c_int32, C.POINTER(C.c_double)]
         lib.eqd_gpu_fp64_fma_peak.restype = C.c_int
         _gpu_lib = lib
@@ -157,6 +162,7 @@ def gpu_lib():
 # Entry points the C ABI must export (checked by the CPU test suite).
 GPU_SYMBOLS = ["eqd_gpu_init", "eqd_gpu_step", "eqd_gpu_fetch", "eqd_gpu_fetch_fault",
                "eqd_gpu_finalize", "eqd_gpu_status_string", "eqd_gpu_stats", "eqd_gpu_time",
-               "eqd_gpu_profile", "eqd_gpu_kernel_time", "eqd_gpu_fp64_fma_peak"]
+               "eqd_gpu_profile", "eqd_gpu_kernel_time", "eqd_gpu_table_info",
+               "eqd_gpu_fp64_fma_peak"]
 CASE_SYMBOLS = ["eqd_case_build", "eqd_case_view", "eqd_case_array_len", "eqd_case_dims",
                 "eqd_case_lines", "eqd_case_free", "eqd_case_last_error"]

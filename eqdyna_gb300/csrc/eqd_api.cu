@@ -12,11 +12,13 @@
 
 #include <algorithm>
 #include <tuple>
+#include <unordered_map>
 
 namespace eqd {
 ElemConst make_elem_const(const Context &c);
 int tile_size_interior();
 int tile_size_pml();
+int record_length(int hg, bool body);
 }  // namespace eqd
 
 using namespace eqd;
@@ -195,6 +197,71 @@ int build_tiles(Context &c, ElemGroup<float> &g, const std::vector<int> &conn_de
 }
 
 std::vector<float> to_f32(const std::vector<double> &v) { return std::vector<float>(v.begin(), v.end()); }
+
+// Distinct binary32 element records: open addressing over a 64-bit hash of the record's bits.
+class RecordDict {
+ public:
+  explicit RecordDict(int len) : len_(len), slots_(1024, -1) {}
+  int len() const { return len_; }
+  long size() const { return (long)hash_.size(); }
+  const std::vector<float> &rows() const { return rows_; }
+  // index of record r (len() floats), added when new; -1 when r is new and `cap` records exist
+  long find_or_add(const float *r, long cap) {
+    const uint64_t h = hash(r);
+    size_t mask = slots_.size() - 1;
+    for (size_t i = h & mask;; i = (i + 1) & mask) {
+      const long q = slots_[i];
+      if (q < 0) {
+        if (size() >= cap) return -1;
+        slots_[i] = size();
+        hash_.push_back(h);
+        rows_.insert(rows_.end(), r, r + len_);
+        if (2 * hash_.size() > slots_.size()) grow();
+        return size() - 1;
+      }
+      if (hash_[q] == h && std::memcmp(&rows_[(size_t)q * len_], r, (size_t)len_ * 4) == 0) return q;
+    }
+  }
+
+ private:
+  uint64_t hash(const float *r) const {
+    uint64_t h = 0x9E3779B97F4A7C15ull;
+    for (int k = 0; k < len_; ++k) {
+      uint32_t w;
+      std::memcpy(&w, r + k, 4);
+      h = (h ^ w) * 0x100000001B3ull;
+      h ^= h >> 29;
+    }
+    return h;
+  }
+  void grow() {
+    std::vector<long> ns(slots_.size() * 2, -1);
+    const size_t mask = ns.size() - 1;
+    for (long q = 0; q < size(); ++q) {
+      size_t i = hash_[q] & mask;
+      while (ns[i] >= 0) i = (i + 1) & mask;
+      ns[i] = q;
+    }
+    slots_.swap(ns);
+  }
+  int len_;
+  std::vector<long> slots_;
+  std::vector<uint64_t> hash_;
+  std::vector<float> rows_;
+};
+
+// Auto layout: record-indexed when a group has at most this many distinct records (the table then
+// stays L2-resident) and at most half as many records as elements.
+constexpr long kAutoMaxRecords = 65536;
+
+// binary32 copy of a component-major table [ncomp][m] with its rows padded with zeros to stride ld
+std::vector<float> to_f32_rows(const std::vector<double> &v, size_t m, size_t ld) {
+  const size_t nc = v.size() / m;
+  std::vector<float> out(nc * ld, 0.f);
+  for (size_t q = 0; q < nc; ++q)
+    for (size_t i = 0; i < m; ++i) out[q * ld + i] = (float)v[q * m + i];
+  return out;
+}
 
 int validate(const eqd_scalars *s, const eqd_host_arrays *a) {
   if (!s || !a) return EQD_ERR_INPUT;
@@ -424,18 +491,99 @@ int build_device_state(eqd_context &X, const eqd_scalars &s, const eqd_host_arra
     if (c.fp32) {
       ElemGroup<float> &h = grp == 0 ? c.gi32 : c.gp32;
       RC(build_tiles(c, h, conn, grp == 0 ? tile_size_interior() : tile_size_pml()));
-      RC(dupload(c, h.shp, to_f32(shp)));
-      RC(dupload(c, h.phi, to_f32(phi)));
-      RC(dupload(c, h.ss, to_f32(ss)));
-      RC(dupload(c, h.detw, to_f32(detw)));
-      RC(dupload(c, h.lam, to_f32(lam)));
-      RC(dupload(c, h.mu, to_f32(mu)));
-      RC(dupload(c, h.stress, to_f32(st)));
-      if (grp == 1 && any_s0) RC(dupload(c, h.stress0, to_f32(st0)));
-      if (grp == 1) RC(dupload(c, h.pml_ab, to_f32(pab)));
-      if (body) RC(dupload(c, h.em, to_f32(em)));
-      if (s.C_hg == 2) RC(dupload(c, h.hgcoef, to_f32(hg)));
-      if (!porep.empty()) RC(dupload(c, h.porep, to_f32(porep)));
+      h.ld = h.ntiles * h.tile;  // whole tiles: every (component, tile) chunk is one aligned bulk copy
+      const size_t um = (size_t)m, ld = (size_t)h.ld;
+      // record-indexed layout: one record per distinct binary32 (geometry, material) combination
+      const int layout = c.opt.table_layout;
+      bool use_rec = layout != EQD_TABLES_STREAMED;
+      RecordDict dict(record_length(s.C_hg, body));
+      std::vector<unsigned> rid, abid;
+      std::vector<float> abt;
+      if (use_rec) {
+        const long cap = layout == EQD_TABLES_RECORDS ? (long)m : std::min<long>(kAutoMaxRecords, m / 2 + 1);
+        rid.assign(ld, 0u);
+        std::vector<float> r(dict.len(), 0.f);
+        for (int i = 0; i < m && use_rec; ++i) {
+          int q = 0;
+          for (int k = 0; k < 24; ++k) r[q++] = (float)shp[k * um + i];
+          if (s.C_hg == 2) {
+            r[q++] = (float)hg[i];
+          } else {
+            for (int k = 0; k < 32; ++k) r[q++] = (float)phi[k * um + i];
+            for (int k = 0; k < 6; ++k) r[q++] = (float)ss[k * um + i];
+          }
+          r[q++] = (float)detw[i];
+          r[q++] = (float)lam[i];
+          r[q++] = (float)mu[i];
+          if (body)
+            for (int k = 0; k < 8; ++k) r[q++] = (float)em[k * um + i];
+          const long id = dict.find_or_add(r.data(), cap);
+          if (id < 0) use_rec = false;
+          else rid[i] = (unsigned)id;
+        }
+      }
+      if (use_rec && grp == 1) {  // PML factors: distinct (a_k, b_k) per axis
+        abid.assign(2 * ld, 0u);
+        std::vector<float> pairs[3];
+        for (int k = 0; k < 3 && use_rec; ++k) {
+          std::unordered_map<uint64_t, unsigned> seen;
+          uint64_t last_key = ~0ull;
+          unsigned last = 0;
+          for (int i = 0; i < m; ++i) {
+            const float fa = (float)pab[k * um + i], fb = (float)pab[(3 + k) * um + i];
+            uint32_t ba, bb;
+            std::memcpy(&ba, &fa, 4);
+            std::memcpy(&bb, &fb, 4);
+            const uint64_t key = (uint64_t)ba | ((uint64_t)bb << 32);
+            if (key != last_key) {
+              auto it = seen.find(key);
+              if (it != seen.end()) {
+                last = it->second;
+              } else {
+                if ((int)seen.size() >= kPmlAxisMax) { use_rec = false; break; }
+                last = (unsigned)seen.size();
+                seen.emplace(key, last);
+                pairs[k].push_back(fa);
+                pairs[k].push_back(fb);
+              }
+              last_key = key;
+            }
+            if (k == 0) abid[i] |= last;
+            else if (k == 1) abid[i] |= last << 16;
+            else abid[ld + i] = last;
+          }
+        }
+        if (use_rec) {
+          h.ab_stride = (int)(std::max({pairs[0].size(), pairs[1].size(), pairs[2].size()}) / 2);
+          abt.assign(3 * (size_t)h.ab_stride * 2, 0.f);
+          for (int k = 0; k < 3; ++k)
+            std::copy(pairs[k].begin(), pairs[k].end(), abt.begin() + 2 * (size_t)k * h.ab_stride);
+        }
+      }
+      if (!use_rec && layout == EQD_TABLES_RECORDS) return EQD_ERR_UNSUPPORTED;
+      if (use_rec) {
+        h.nrec = (int)dict.size();
+        h.rec_len = dict.len();
+        RC(dupload(c, h.rec, dict.rows()));
+        RC(dupload(c, h.rec_id, rid));
+        if (grp == 1) {
+          RC(dupload(c, h.ab_id, abid));
+          RC(dupload(c, h.ab_tab, abt));
+        }
+      } else {
+        RC(dupload(c, h.shp, to_f32_rows(shp, um, ld)));
+        RC(dupload(c, h.phi, to_f32_rows(phi, um, ld)));
+        RC(dupload(c, h.ss, to_f32_rows(ss, um, ld)));
+        RC(dupload(c, h.detw, to_f32_rows(detw, um, ld)));
+        RC(dupload(c, h.lam, to_f32_rows(lam, um, ld)));
+        RC(dupload(c, h.mu, to_f32_rows(mu, um, ld)));
+        if (grp == 1) RC(dupload(c, h.pml_ab, to_f32_rows(pab, um, ld)));
+        if (body) RC(dupload(c, h.em, to_f32_rows(em, um, ld)));
+        if (s.C_hg == 2) RC(dupload(c, h.hgcoef, to_f32_rows(hg, um, ld)));
+      }
+      RC(dupload(c, h.stress, to_f32_rows(st, um, ld)));
+      if (grp == 1 && any_s0) RC(dupload(c, h.stress0, to_f32_rows(st0, um, ld)));
+      if (!porep.empty()) RC(dupload(c, h.porep, to_f32_rows(porep, um, ld)));
       if (!pstr.empty()) RC(dupload(c, h.pstrain, pstr));
       continue;
     }
@@ -765,6 +913,7 @@ int eqd_gpu_step(eqd_context *X, int32_t nt_begin, int32_t nsteps) {
   c.time = X->times[c.nt];
   c.launches_last = launches;
   c.elem_updates += (int64_t)c.nelem * nsteps;
+  if (err & 2) return EQD_ERR_TIMEOUT;
   if (err) return EQD_ERR_NAN;
   return EQD_OK;
 }
@@ -865,10 +1014,11 @@ int eqd_gpu_fetch(eqd_context *X, eqd_host_arrays *a) {
       const int nstress = grp == 0 ? (c.sc.C_Q == 1 ? 12 : 6) : 15;
       std::vector<double> st(nstress * (size_t)m);
       if (c.fp32) {
-        std::vector<float> s32(st.size());
         const ElemGroup<float> &g = grp == 0 ? c.gi32 : c.gp32;
+        std::vector<float> s32(nstress * (size_t)g.ld);
         EQD_CUDA_OK(cudaMemcpy(s32.data(), g.stress, s32.size() * 4, cudaMemcpyDeviceToHost));
-        for (size_t q = 0; q < st.size(); ++q) st[q] = s32[q];
+        for (int q = 0; q < nstress; ++q)
+          for (int i = 0; i < m; ++i) st[q * (size_t)m + i] = s32[q * (size_t)g.ld + i];
       } else {
         const ElemGroup<double> &g = grp == 0 ? c.gi64 : c.gp64;
         EQD_CUDA_OK(cudaMemcpy(st.data(), g.stress, st.size() * 8, cudaMemcpyDeviceToHost));
@@ -952,6 +1102,18 @@ int eqd_gpu_kernel_time(eqd_context *X, int32_t kind, double *ms, int64_t *launc
   if (kind < 0 || kind > 4) return EQD_ERR_INPUT;
   if (ms) *ms = X->c.prof_ms[kind];
   if (launches) *launches = X->c.prof_launches[kind];
+  return EQD_OK;
+}
+
+int eqd_gpu_table_info(eqd_context *X, int32_t group, int64_t info[4]) {
+  if (!X) return EQD_ERR_STATE;
+  if ((group != 0 && group != 1) || !info) return EQD_ERR_INPUT;
+  const Context &c = X->c;
+  const ElemGroup<float> &g = group == 0 ? c.gi32 : c.gp32;
+  info[0] = (!c.fp32 || g.ne == 0) ? 0 : (g.nrec > 0 ? 2 : 1);
+  info[1] = c.fp32 ? g.ne : (group == 0 ? c.gi64.ne : c.gp64.ne);
+  info[2] = g.nrec;
+  info[3] = g.rec_len;
   return EQD_OK;
 }
 

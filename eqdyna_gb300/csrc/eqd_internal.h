@@ -49,8 +49,20 @@ struct ElemGroup {
   int *tile_nodes = nullptr;        // device node ids, sorted, per tile
   unsigned short *tile_incp = nullptr;  // per tile: M + 1 offsets into that tile's incidences
   int *tile_incp_off = nullptr;     // [ntiles + 1] offsets into tile_incp
-  unsigned short *tile_inc = nullptr;   // [ntiles * tile * 8] incidences (e_local * 8 + corner)
+  unsigned short *tile_inc = nullptr;   // [ntiles * tile * 8] incidences (corner * tile + e_local)
+  // record-indexed binary32 tables (nrec > 0): elements with bit-identical geometry and material
+  // share one record [shp 24 | phi 32, ss 6 (or hgcoef 1) | detw, lam, mu | em 8], and the
+  // per-element tables above (shp ... em, pml_ab) are not allocated
+  int nrec = 0, rec_len = 0;        // records, floats per record (a multiple of 4)
+  float *rec = nullptr;             // [nrec][rec_len]
+  unsigned *rec_id = nullptr;       // [ld] record of each element
+  unsigned *ab_id = nullptr;        // PML [2][ld]: indices of (a_k, b_k) in ab_tab, 16 bits per
+                                    // axis: row 0 = i_x | i_y << 16, row 1 = i_z
+  float *ab_tab = nullptr;          // PML [3][ab_stride][2]
+  int ab_stride = 0;                // distinct (a_k, b_k) pairs of the most varied axis
 };
+
+constexpr int kPmlAxisMax = 65536;  // distinct PML factor pairs per axis in the record layout
 
 struct PairStation {
   int pair;      // 0-based pair index
@@ -98,7 +110,7 @@ struct Context {
   // step bookkeeping
   int *d_nt = nullptr;          // current step index on the device
   double *d_times = nullptr;    // [nstep + 2] timeElapsed after nt steps
-  int *d_err = nullptr;         // error word: 1 = NaN velocity
+  int *d_err = nullptr;         // error word: 1 = NaN velocity, 2 = bounded wait gave up
   unsigned long long *d_stats = nullptr;  // [4]: newton iterations, ivmax hits, ...
   int nt = 0;                   // steps completed (host mirror)
   double time = 0.0;

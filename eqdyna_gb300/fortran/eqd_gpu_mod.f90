@@ -7,6 +7,7 @@ module eqd_gpu_mod
 
   integer(c_int), parameter :: EQD_OK = 0, EQD_ERR_NAN = 4
   integer(c_int), parameter :: EQD_PREC_FP64 = 0, EQD_PREC_FP32 = 1
+  integer(c_int), parameter :: EQD_TABLES_AUTO = 0, EQD_TABLES_STREAMED = 1, EQD_TABLES_RECORDS = 2
 
   type, bind(C) :: eqd_scalars
     real(c_double) :: dt, rdampk, rdampm, grav, roumax, rhow, gamar, w, kapa_hg
@@ -32,7 +33,7 @@ module eqd_gpu_mod
 
   type, bind(C) :: eqd_options
     integer(c_int32_t) :: precision, learned_guess, record_tp_hist, block_elem
-    integer(c_int32_t) :: use_graph, device, reserved(2)
+    integer(c_int32_t) :: use_graph, device, table_layout, reserved
   end type
 
   interface

@@ -19,7 +19,7 @@ PRECISIONS = {"fp64": N.PREC_FP64, "fp32": N.PREC_FP32}
 
 class GpuSolver:
     def __init__(self, case, precision="fp64", learned_guess=False, use_graph=True, device=0,
-                 record_tp_hist=False):
+                 record_tp_hist=False, table_layout="auto"):
         self.lib = N.gpu_lib()
         self.case = case
         self._ha = case.host_arrays()
@@ -29,6 +29,7 @@ class GpuSolver:
         opt.record_tp_hist = int(bool(record_tp_hist))
         opt.use_graph = int(bool(use_graph))
         opt.device = int(device)
+        opt.table_layout = N.TABLE_LAYOUTS[table_layout]
         self._opt = opt
         h = C.c_void_p()
         rc = self.lib.eqd_gpu_init(C.byref(case.scalars), C.byref(self._ha), C.byref(opt), C.byref(h))
@@ -82,6 +83,19 @@ class GpuSolver:
             ms, n = C.c_double(), C.c_int64()
             self.lib.eqd_gpu_kernel_time(self._h, k, C.byref(ms), C.byref(n))
             out[name] = (ms.value, n.value)
+        return out
+
+    def table_info(self):
+        """Binary32 element-table layout per group: {"interior"|"pml": {layout, elements, records,
+        record_floats}}; layout is "records", "streamed" or None (empty group / binary64 form)."""
+        out = {}
+        for name, grp in (("interior", 0), ("pml", 1)):
+            info = (C.c_int64 * 4)()
+            rc = self.lib.eqd_gpu_table_info(self._h, grp, info)
+            if rc != 0:
+                raise N.EqdError(rc, "eqd_gpu_table_info")
+            out[name] = {"layout": {0: None, 1: "streamed", 2: "records"}[info[0]], "elements": info[1],
+                         "records": info[2], "record_floats": info[3]}
         return out
 
     @property

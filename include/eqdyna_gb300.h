@@ -113,6 +113,14 @@ enum eqd_precision {
                              binary32 nodal accumulation; state, fault and Newton in binary64  */
 };
 
+/* Element-table layout of the binary32 form (results are identical in both layouts). */
+enum eqd_table_layout {
+  EQD_TABLES_AUTO = 0,     /* per element group: records when it has few distinct records      */
+  EQD_TABLES_STREAMED = 1, /* every element keeps its own geometry / material tables           */
+  EQD_TABLES_RECORDS = 2   /* elements index a table of distinct (geometry, material) records;
+                              EQD_ERR_UNSUPPORTED if a PML axis has > 65536 distinct factors    */
+};
+
 typedef struct eqd_options {
   int32_t precision;      /* enum eqd_precision                                                */
   int32_t learned_guess;  /* 1: MLP initial guess for the rate-and-state Newton (friclaw 3/4)  */
@@ -120,7 +128,8 @@ typedef struct eqd_options {
   int32_t block_elem;     /* element-kernel block size, 0 = autotuned default                  */
   int32_t use_graph;      /* 1: capture the multi-step loop in a CUDA graph                    */
   int32_t device;         /* CUDA device ordinal                                               */
-  int32_t reserved[2];
+  int32_t table_layout;   /* enum eqd_table_layout (binary32 form only)                        */
+  int32_t reserved;
 } eqd_options;
 
 typedef struct eqd_context eqd_context;
@@ -165,6 +174,11 @@ int eqd_gpu_profile(eqd_context *ctx, int32_t enable);
 /* Milliseconds and launch count accumulated while profiling, per kind:
  * 0 whole steps, 1 node update, 2 interior elements, 3 PML elements, 4 fault + stations. */
 int eqd_gpu_kernel_time(eqd_context *ctx, int32_t kind, double *ms, int64_t *launches);
+
+/* Element-table layout of the binary32 form for group 0 (interior) or 1 (PML):
+ * info[0] = 2 record-indexed, 1 streamed, 0 group empty or binary64 form; info[1] = elements;
+ * info[2] = distinct records; info[3] = floats per record (both 0 when streamed). */
+int eqd_gpu_table_info(eqd_context *ctx, int32_t group, int64_t info[4]);
 
 /* Measured binary64 fused-multiply-add throughput of a device (TFLOP/s, 2 flops per FMA),
  * from a register-resident FMA chain kernel; used as the compute roofline of the FP64 form. */
