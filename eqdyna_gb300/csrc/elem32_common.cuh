@@ -393,15 +393,15 @@ __device__ __forceinline__ void pml_element(const Src &S, const float *sv, const
 }
 
 // PML gather: one thread per tile node; the split-field forces of an incidence are rebuilt from
-// the element's det * shape gradient (SrcOf(el) gives the table source of local element el) and
-// its split-stress sums.  12-DOF nodes reduce 9 split components + 3 into F9 / F; 3-DOF nodes on
-// the PML boundary take the compensated sum of their 4 partials.
-template <int HG, class SrcOf>
+// the element's det * shape gradient of the corner (w_of(el, a, wx, wy, wz) for local element el,
+// corner a: the binary32 products dw * shp, as in pml_element) and its split-stress sums.
+// 12-DOF nodes reduce 9 split components + 3 into F9 / F; 3-DOF nodes on the PML boundary take
+// the compensated sum of their 4 partials.
+template <class WOf>
 __device__ __forceinline__ void pml_gather(const ElemGroup<float> &g, int M, int nb, const unsigned short *incp,
                                            const unsigned short *sinc, const float *es, const float *cfh,
-                                           const SrcOf &src_of, float *__restrict__ F, float *__restrict__ F9,
+                                           const WOf &w_of, float *__restrict__ F, float *__restrict__ F9,
                                            int nnode, int n_int, int npml) {
-  using C = TabCommon<HG>;
   for (int j = threadIdx.x; j < M; j += blockDim.x) {
     float hi[12], lo[12];
 #pragma unroll
@@ -410,10 +410,8 @@ __device__ __forceinline__ void pml_gather(const ElemGroup<float> &g, int M, int
     for (int q = incp[j]; q < q1; ++q) {
       const int r = sinc[q];
       const int a = r / kTile, el = r - a * kTile;
-      const auto S = src_of(el);
-      const float dw = S.g(C::DET);
-      const float wx = dw * S.g(C::SHP + 3 * a), wy = dw * S.g(C::SHP + 3 * a + 1);
-      const float wz = dw * S.g(C::SHP + 3 * a + 2);
+      float wx, wy, wz;
+      w_of(el, a, wx, wy, wz);
       const float sxx = es[el], syy = es[kTile + el], szz = es[2 * kTile + el];
       const float sxy = es[3 * kTile + el], sxz = es[4 * kTile + el], syz = es[5 * kTile + el];
       const float f9[9] = {-wx * sxx, -wy * sxy, -wz * sxz, -wx * sxy, -wy * syy,
@@ -442,6 +440,24 @@ __device__ __forceinline__ void pml_gather(const ElemGroup<float> &g, int M, int
       }
     }
   }
+}
+
+// w_of for table sources: dw * shape gradient of corner a of the element that src_of(el) reads.
+template <int HG, class SrcOf>
+struct WFromSrc {
+  SrcOf src_of;
+  __device__ void operator()(int el, int a, float &wx, float &wy, float &wz) const {
+    using C = TabCommon<HG>;
+    const auto S = src_of(el);
+    const float dw = S.g(C::DET);
+    wx = dw * S.g(C::SHP + 3 * a);
+    wy = dw * S.g(C::SHP + 3 * a + 1);
+    wz = dw * S.g(C::SHP + 3 * a + 2);
+  }
+};
+template <int HG, class SrcOf>
+__device__ __forceinline__ WFromSrc<HG, SrcOf> w_from_src(const SrcOf &f) {
+  return WFromSrc<HG, SrcOf>{f};
 }
 
 template <class K>

@@ -155,8 +155,9 @@ void brick_order(const eqd_host_arrays &a, std::vector<int> &ids, int bx, int bz
   for (size_t i = 0; i < m; ++i) ids[i] = std::get<6>(keys[i]);
 }
 
-// Tile metadata: per tile its distinct nodes (sorted device ids) and, per node, the incidences
-// (corner * tile + local element) in ascending order.
+// Tile metadata: per tile its distinct nodes and, per node, the incidences (corner * tile + local
+// element) in ascending order.  Nodes are ordered by incidence count (most first), then by device
+// id, so the 32 nodes of a warp in the gather loop have (nearly) the same trip count.
 int build_tiles(Context &c, ElemGroup<float> &g, const std::vector<int> &conn_dev, int tile) {
   const int m = g.ne;
   g.tile = tile;
@@ -171,15 +172,21 @@ int build_tiles(Context &c, ElemGroup<float> &g, const std::vector<int> &conn_de
     for (int e = e0; e < e1; ++e)
       for (int q = 0; q < 8; ++q) pairs.push_back({conn_dev[(size_t)q * m + e], q * tile + (e - e0)});
     std::sort(pairs.begin(), pairs.end());
+    std::vector<std::pair<size_t, size_t>> runs;  // [first, last) of each node's incidences
+    for (size_t k = 0; k < pairs.size(); ++k)
+      if (k == 0 || pairs[k].first != pairs[k - 1].first) runs.push_back({k, k});
+    for (size_t r = 0; r < runs.size(); ++r) runs[r].second = r + 1 < runs.size() ? runs[r + 1].first : pairs.size();
+    std::stable_sort(runs.begin(), runs.end(), [](const std::pair<size_t, size_t> &x, const std::pair<size_t, size_t> &y) {
+      return x.second - x.first > y.second - y.first;
+    });
     int M = 0;
     const size_t base = (size_t)t * tile * 8;
-    for (size_t k = 0; k < pairs.size(); ++k) {
-      if (k == 0 || pairs[k].first != pairs[k - 1].first) {
-        nodes.push_back(pairs[k].first);
-        incp.push_back((unsigned short)k);
-        ++M;
-      }
-      inc[base + k] = (unsigned short)pairs[k].second;
+    size_t k = 0;
+    for (const auto &run : runs) {
+      nodes.push_back(pairs[run.first].first);
+      incp.push_back((unsigned short)k);
+      ++M;
+      for (size_t q = run.first; q < run.second; ++q) inc[base + k++] = (unsigned short)pairs[q].second;
     }
     incp.push_back((unsigned short)pairs.size());
     node_ptr.push_back((int)nodes.size());
@@ -564,6 +571,7 @@ int build_device_state(eqd_context &X, const eqd_scalars &s, const eqd_host_arra
       if (use_rec) {
         h.nrec = (int)dict.size();
         h.rec_len = dict.len();
+        std::copy(dict.rows().begin(), dict.rows().begin() + dict.len(), c.rec0[grp].v);
         RC(dupload(c, h.rec, dict.rows()));
         RC(dupload(c, h.rec_id, rid));
         if (grp == 1) {

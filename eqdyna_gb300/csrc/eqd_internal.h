@@ -63,6 +63,12 @@ struct ElemGroup {
 };
 
 constexpr int kPmlAxisMax = 65536;  // distinct PML factor pairs per axis in the record layout
+constexpr int kRecMax = 80;         // floats of the longest element record
+
+// The record of a group that has exactly one (uniform grid), passed to its kernels by value.
+struct RecordParam {
+  float v[kRecMax];
+};
 
 struct PairStation {
   int pair;      // 0-based pair index
@@ -94,6 +100,7 @@ struct Context {
   // elements
   ElemGroup<double> gi64, gp64;
   ElemGroup<float> gi32, gp32;
+  RecordParam rec0[2] = {};     // host copy of record 0 of each binary32 group (used when nrec == 1)
   int *elem_type_host = nullptr;
   // fault
   int *pair_s = nullptr, *pair_m = nullptr;  // device node ids

@@ -156,7 +156,7 @@ __global__ void __launch_bounds__(kTile)
                               es, cfh);
   __syncthreads();
   auto src_of = [&](int el) { return SlabSrc<L>{tab, el}; };
-  pml_gather<HG>(g, M, nb, incp, sinc, es, cfh, src_of, F, F9, nnode, n_int, npml);
+  pml_gather(g, M, nb, incp, sinc, es, cfh, w_from_src<HG>(src_of), F, F9, nnode, n_int, npml);
 }
 
 template <class L>

@@ -9,6 +9,10 @@
 // bit-identical to the streamed layout's; results differ only through the order of the binary32
 // L2 reductions.
 //
+// A group with a single record (a uniform grid) runs the UNI variant: the record is a kernel
+// parameter (__grid_constant__), so its values are constant-bank operands with no load
+// instruction, and the PML gather reads the 24 products det * shape gradient from shared memory.
+//
 // Per tile (CTA of 128 elements): one elected thread bulk-copies the per-element rows that remain
 // (stress, record index, PML axis indices, initial stress, pore pressure) and the incidence list
 // into shared memory while all threads gather the tile's node data; then the element math and the
@@ -64,14 +68,36 @@ struct RecSrc {
   __device__ float pb(int k) const { return __ldg(abt + 2 * ab_index(k) + 1); }
 };
 
+// Table source of a group with one record, held in the kernel's parameter space.
+template <class L>
+struct UniSrc {
+  const RecordParam &r;
+  const float *tab;
+  int col;
+  const float *abt;
+  int stride;
+  unsigned ab01, ab2;
+  __device__ float g(int row) const { return r.v[row]; }
+  __device__ float em(int a) const { return r.v[L::REM + a]; }
+  __device__ float str(int i) const { return tab[(L::STR + i) * kTile + col]; }
+  __device__ float por() const { return tab[L::POR * kTile + col]; }
+  __device__ float st0(int i) const { return tab[(L::ST0 + i) * kTile + col]; }
+  __device__ int ab_index(int k) const {
+    return k * stride + (int)(k == 0 ? (ab01 & 0xFFFFu) : (k == 1 ? (ab01 >> 16) : ab2));
+  }
+  __device__ float pa(int k) const { return __ldg(abt + 2 * ab_index(k)); }
+  __device__ float pb(int k) const { return __ldg(abt + 2 * ab_index(k) + 1); }
+};
+
 __device__ __forceinline__ unsigned row_u32(const float *tab, int row, int col) {
   return reinterpret_cast<const unsigned *>(tab)[row * kTile + col];
 }
 
-template <bool BODY, bool PLASTIC, int HG>
+template <bool BODY, bool PLASTIC, int HG, bool UNI>
 __global__ void __launch_bounds__(kTile)
     elem_interior_rec(ElemGroup<float> g, const float *__restrict__ vel32, const float *__restrict__ dl32,
-                      float *__restrict__ F, int nnode, ElemConst32 k, int *__restrict__ err) {
+                      float *__restrict__ F, int nnode, ElemConst32 k, int *__restrict__ err,
+                      const __grid_constant__ RecordParam rp) {
   using L = RecInterior<BODY, PLASTIC, HG>;
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) unsigned long long bar;
@@ -102,22 +128,29 @@ __global__ void __launch_bounds__(kTile)
   const int e = e0 + tid;
   float *fs = tab + L::FS * kTile;
   if (e < g.ne) {
-    const RecSrc<L> S{g.rec + (size_t)row_u32(tab, L::RID, tid) * g.rec_len, tab, tid, nullptr, 0, 0u, 0u};
-    interior_element<BODY, PLASTIC, HG>(S, sv, sd, Mmax, slot_of, tid, k, PLASTIC ? g.pstrain + e : nullptr,
-                                        g.stress + e, (size_t)ld, fs);
+    double *ps = PLASTIC ? g.pstrain + e : nullptr;
+    if (UNI) {
+      const UniSrc<L> S{rp, tab, tid, nullptr, 0, 0u, 0u};
+      interior_element<BODY, PLASTIC, HG>(S, sv, sd, Mmax, slot_of, tid, k, ps, g.stress + e, (size_t)ld, fs);
+    } else {
+      const RecSrc<L> S{g.rec + (size_t)row_u32(tab, L::RID, tid) * g.rec_len, tab, tid, nullptr, 0, 0u, 0u};
+      interior_element<BODY, PLASTIC, HG>(S, sv, sd, Mmax, slot_of, tid, k, ps, g.stress + e, (size_t)ld, fs);
+    }
   }
   __syncthreads();
   interior_gather(g, M, nb, incp, sinc, fs, F, nnode);
 }
 
-template <bool BODY, bool S0, int HG>
+template <bool BODY, bool S0, int HG, bool UNI>
 __global__ void __launch_bounds__(kTile)
     elem_pml_rec(ElemGroup<float> g, const float *__restrict__ vel32, const float *__restrict__ dl32,
                  float *__restrict__ F, float *__restrict__ F9, int nnode, int n_int, int npml,
-                 ElemConst32 k, int *__restrict__ err) {
+                 ElemConst32 k, int *__restrict__ err, const __grid_constant__ RecordParam rp) {
   using L = RecPml<BODY, S0, HG>;
+  using C = TabCommon<HG>;
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) unsigned long long bar;
+  __shared__ float cw[24];  // UNI: det * shape gradient (3 a + k) of the group's record
   const int Mmax = g.max_tile_nodes;
   float *tab = reinterpret_cast<float *>(smem);
   unsigned short *sinc = reinterpret_cast<unsigned short *>(tab + L::NS * kTile);
@@ -136,6 +169,7 @@ __global__ void __launch_bounds__(kTile)
     copy_rows(tab, L::RID, g.rec_id, 1, ld, e0, &bar);
     copy_rows(tab, L::ABID, g.ab_id, 2, ld, e0, &bar);
   }
+  if (UNI && tid < 24) cw[tid] = rp.v[C::DET] * rp.v[C::SHP + tid];
   __syncthreads();
   int nb;
   const int M = stage_nodes(g, vel32, dl32, nnode, Mmax, sv, sd, nb);
@@ -149,15 +183,30 @@ __global__ void __launch_bounds__(kTile)
   const float *rec = g.rec;
   const int rlen = g.rec_len;
   if (e < g.ne) {
-    const RecSrc<L> S{rec + (size_t)row_u32(tab, L::RID, tid) * rlen, tab, tid, g.ab_tab, g.ab_stride,
-                      row_u32(tab, L::ABID, tid), row_u32(tab, L::ABID + 1, tid)};
-    pml_element<BODY, S0, HG>(S, sv, sd, Mmax, slot_of, tid, k, g.stress + e, (size_t)ld, es, cfh);
+    const unsigned ab01 = row_u32(tab, L::ABID, tid), ab2 = row_u32(tab, L::ABID + 1, tid);
+    if (UNI) {
+      const UniSrc<L> S{rp, tab, tid, g.ab_tab, g.ab_stride, ab01, ab2};
+      pml_element<BODY, S0, HG>(S, sv, sd, Mmax, slot_of, tid, k, g.stress + e, (size_t)ld, es, cfh);
+    } else {
+      const RecSrc<L> S{rec + (size_t)row_u32(tab, L::RID, tid) * rlen, tab, tid, g.ab_tab, g.ab_stride,
+                        ab01, ab2};
+      pml_element<BODY, S0, HG>(S, sv, sd, Mmax, slot_of, tid, k, g.stress + e, (size_t)ld, es, cfh);
+    }
   }
   __syncthreads();
-  auto src_of = [&](int el) {
-    return RecSrc<L>{rec + (size_t)row_u32(tab, L::RID, el) * rlen, tab, el, nullptr, 0, 0u, 0u};
-  };
-  pml_gather<HG>(g, M, nb, incp, sinc, es, cfh, src_of, F, F9, nnode, n_int, npml);
+  if (UNI) {
+    auto w_of = [&](int, int a, float &wx, float &wy, float &wz) {
+      wx = cw[3 * a];
+      wy = cw[3 * a + 1];
+      wz = cw[3 * a + 2];
+    };
+    pml_gather(g, M, nb, incp, sinc, es, cfh, w_of, F, F9, nnode, n_int, npml);
+  } else {
+    auto src_of = [&](int el) {
+      return RecSrc<L>{rec + (size_t)row_u32(tab, L::RID, el) * rlen, tab, el, nullptr, 0, 0u, 0u};
+    };
+    pml_gather(g, M, nb, incp, sinc, es, cfh, w_from_src<HG>(src_of), F, F9, nnode, n_int, npml);
+  }
 }
 
 template <class L>
@@ -165,24 +214,34 @@ size_t rec_smem(int Mmax) {
   return (size_t)L::NS * kTile * 4 + 2 * (8 * kTile * 2) + 6 * (size_t)Mmax * 4;
 }
 
-template <bool BODY, bool PLASTIC, int HG>
-int launch_interior(Context &c, cudaStream_t s, const ElemConst32 &k) {
+template <bool BODY, bool PLASTIC, int HG, bool UNI>
+int launch_interior_v(Context &c, cudaStream_t s, const ElemConst32 &k) {
   const ElemGroup<float> &g = c.gi32;
   const size_t sm = rec_smem<RecInterior<BODY, PLASTIC, HG>>(g.max_tile_nodes);
-  auto kern = elem_interior_rec<BODY, PLASTIC, HG>;
+  auto kern = elem_interior_rec<BODY, PLASTIC, HG, UNI>;
   if (allow_smem(kern, sm)) return EQD_ERR_CUDA;
-  kern<<<g.ntiles, kTile, sm, s>>>(g, c.vel32, c.dl32, c.F32, c.nnode, k, c.d_err);
+  kern<<<g.ntiles, kTile, sm, s>>>(g, c.vel32, c.dl32, c.F32, c.nnode, k, c.d_err, c.rec0[0]);
   return EQD_OK;
 }
+template <bool BODY, bool PLASTIC, int HG>
+int launch_interior(Context &c, cudaStream_t s, const ElemConst32 &k) {
+  return c.gi32.nrec == 1 ? launch_interior_v<BODY, PLASTIC, HG, true>(c, s, k)
+                          : launch_interior_v<BODY, PLASTIC, HG, false>(c, s, k);
+}
 
-template <bool BODY, bool S0, int HG>
-int launch_pml(Context &c, cudaStream_t s, const ElemConst32 &k) {
+template <bool BODY, bool S0, int HG, bool UNI>
+int launch_pml_v(Context &c, cudaStream_t s, const ElemConst32 &k) {
   const ElemGroup<float> &g = c.gp32;
   const size_t sm = rec_smem<RecPml<BODY, S0, HG>>(g.max_tile_nodes);
-  auto kern = elem_pml_rec<BODY, S0, HG>;
+  auto kern = elem_pml_rec<BODY, S0, HG, UNI>;
   if (allow_smem(kern, sm)) return EQD_ERR_CUDA;
-  kern<<<g.ntiles, kTile, sm, s>>>(g, c.vel32, c.dl32, c.F32, c.F9_32, c.nnode, c.n_int, c.npml, k, c.d_err);
+  kern<<<g.ntiles, kTile, sm, s>>>(g, c.vel32, c.dl32, c.F32, c.F9_32, c.nnode, c.n_int, c.npml, k, c.d_err,
+                                   c.rec0[1]);
   return EQD_OK;
+}
+template <bool BODY, bool S0, int HG>
+int launch_pml(Context &c, cudaStream_t s, const ElemConst32 &k) {
+  return c.gp32.nrec == 1 ? launch_pml_v<BODY, S0, HG, true>(c, s, k) : launch_pml_v<BODY, S0, HG, false>(c, s, k);
 }
 
 template <int HG>
@@ -202,6 +261,7 @@ int launch_hg(Context &c, cudaStream_t s, const ElemConst32 &k, bool interior) {
 
 int record_length(int hg, bool body) {
   const int n = (hg == 2 ? TabCommon<2>::STR : TabCommon<1>::STR) + (body ? 8 : 0);
+  static_assert(TabCommon<1>::STR + 8 <= kRecMax, "record longer than RecordParam");
   return (n + 3) / 4 * 4;
 }
 
