@@ -248,36 +248,40 @@ def bench_ours(args, world, rank, local):
     lib = N.gpu_lib()
     t_setup = time.perf_counter()
     tmp = tempfile.mkdtemp(prefix="eqd_bench_")
-    total_steps = 2 * (args.steps + args.warmup) + 4
+    total_steps = 2 * (args.steps + args.warmup) + 4 + (args.log_steps * args.log_stride if args.learned else 0)
     case = build_case(args.config, args.scale, total_steps, tmp)
     shutil.rmtree(tmp, ignore_errors=True)
     ne = case.sizes["nelem"]
     host_bytes_in = sum(v.nbytes for k, v in case.arrays.items() if v is not None)
     setup_s = time.perf_counter() - t_setup
 
-    # ---- end to end through the C ABI with host buffers ----
-    e2e_case = case.clone()
-    fr = np.zeros_like(e2e_case.arrays["fric"])
-    fn = np.zeros_like(e2e_case.arrays["fnft"])
-    barrier(world)
-    t0 = time.perf_counter()
-    s = GpuSolver(e2e_case, precision=args.precision, learned_guess=args.learned, device=local,
-                  table_layout=args.tables)
-    for _ in range(args.steps):
-        s.step(1)
-        s.fetch_fault(fr, fn)
-    s.fetch()
-    e2e_s = time.perf_counter() - t0
-    s.close()
-    e2e_s = allreduce_max(e2e_s, world)
-    del e2e_case
     npair = case.npair
     d2h_per_step = 100 * npair * 8 + npair * 8
+    args.learned = int(bool(args.learned) and case.scalars.friclaw in (3, 4))  # rate-and-state only
 
-    # ---- device-timed steps ----
-    s = GpuSolver(case, precision=args.precision, learned_guess=args.learned, device=local,
+    # ---- device-timed steps (inputs resident in HBM) ----
+    s = GpuSolver(case.clone(), precision=args.precision, learned_guess=args.learned, device=local,
                   table_layout=args.tables)
+    learned = None
+    if args.learned:
+        # seeded warm-up of the plain method whose Newton solves are the training data
+        t0 = time.perf_counter()
+        s.newton_log(args.log_steps, args.log_stride)
+        s.step(args.log_steps * args.log_stride)
+        warm_s = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        hist = s.train_mlp(epochs=args.epochs, batch=4096, lr=1e-3, holdout=0.05, seed=20261203)
+        train_s = time.perf_counter() - t0
+        plain = s.replay(learned=False)
+        guess = s.replay(learned=True)
+        params, norm = s.mlp_state()
+        learned = {"records": plain["records"], "warmup_steps": args.log_steps * args.log_stride,
+                   "log_stride": args.log_stride, "warmup_s": round(warm_s, 2), "train_s": round(train_s, 2),
+                   "epochs": args.epochs, "epoch_loss": [round(x, 5) for x in hist["epoch_loss"]],
+                   "holdout_loss": round(hist["holdout_loss"], 5),
+                   "replay_plain_guess": plain, "replay_learned_guess": guess}
     s.step(args.warmup)
+    n_before = s.newton_counts()
     s.profile(True, reset=True)
     barrier(world)
     with ClockSampler(local) as clk:
@@ -288,12 +292,33 @@ def bench_ours(args, world, rank, local):
     s.profile(False)
     kt = s.kernel_times()
     stats = s.stats()
+    n_after = s.newton_counts()
+    newton = {k: n_after[k] - n_before[k] for k in n_after}
     tables = s.table_info()
     step_ms_total = kt["step"][0]
     dev_s = allreduce_max(step_ms_total / 1e3, world)
     units = allreduce_sum(float(ne) * args.steps, world)
     value = units / dev_s
     s.close()
+
+    # ---- end to end through the C ABI with host buffers ----
+    e2e_case = case.clone()
+    fr = np.zeros_like(e2e_case.arrays["fric"])
+    fn = np.zeros_like(e2e_case.arrays["fnft"])
+    barrier(world)
+    t0 = time.perf_counter()
+    s = GpuSolver(e2e_case, precision=args.precision, learned_guess=args.learned, device=local,
+                  table_layout=args.tables)
+    if args.learned:
+        s.set_mlp(params, norm)
+    for _ in range(args.steps):
+        s.step(1)
+        s.fetch_fault(fr, fn)
+    s.fetch()
+    e2e_s = time.perf_counter() - t0
+    s.close()
+    e2e_s = allreduce_max(e2e_s, world)
+    del e2e_case
 
     # ---- roofline of the dominant kernel ----
     hbm_peak, peak_kind = _peaks()
@@ -338,7 +363,8 @@ def bench_ours(args, world, rank, local):
                     "d2h_bytes_per_step": int(d2h_per_step + host_bytes_in / args.steps),
                     "note": "init (every table host->device) + per-step fault-state read + final fetch"},
             "gpu_launches": int(stats["kernel_launches"]),
-            "newton": {"iters": stats["newton_iters"], "ivmax_hits": stats["newton_maxhits"]},
+            "newton": newton,
+            "learned": learned,
             "roofline": roofline, "clocks": clk.summary()}
     if cpu:
         line["cpu_baseline"] = cpu
@@ -353,7 +379,10 @@ def main():
     ap.add_argument("--config", default="C1")
     ap.add_argument("--scale", type=float, default=1.0)
     ap.add_argument("--precision", default="fp32", choices=["fp64", "fp32"])
-    ap.add_argument("--learned", type=int, default=0)
+    ap.add_argument("--learned", type=int, default=1, help="learned Newton initial guess (rate-and-state)")
+    ap.add_argument("--log-steps", type=int, default=70, help="logged warm-up steps (training data)")
+    ap.add_argument("--log-stride", type=int, default=10, help="one logged step in this many")
+    ap.add_argument("--epochs", type=int, default=8)
     ap.add_argument("--tables", default="auto", choices=["auto", "streamed", "records"],
                     help="binary32 element-table layout")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])

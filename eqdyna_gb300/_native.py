@@ -78,6 +78,15 @@ PREC_FP32 = 1
 
 TABLE_LAYOUTS = {"auto": 0, "streamed": 1, "records": 2}
 
+NEWTON_RECORD = 16
+MLP_PARAMS = 5313
+MLP_NORM = 18
+
+
+class MlpTrainOptions(C.Structure):
+    _fields_ = [("epochs", C.c_int32), ("batch", C.c_int32), ("lr", C.c_float), ("holdout", C.c_float),
+                ("seed", C.c_uint64)]
+
 STATUS = {0: "ok", 1: "bad input", 2: "CUDA error", 3: "device out of memory", 4: "NaN velocity",
           5: "unsupported option", 6: "no CUDA device", 7: "bounded wait timed out",
           8: "call out of order"}
@@ -151,6 +160,20 @@ def gpu_lib():
         lib.eqd_gpu_kernel_time.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_double),
                                             C.POINTER(C.c_int64)]
         lib.eqd_gpu_kernel_time.restype = C.c_int
+        f_p, d_p, i64_p = C.POINTER(C.c_float), C.POINTER(C.c_double), C.POINTER(C.c_int64)
+        lib.eqd_gpu_newton_log.argtypes = [C.c_void_p, C.c_int32, C.c_int32]
+        lib.eqd_gpu_newton_records.argtypes = [C.c_void_p, d_p, C.c_int64, i64_p]
+        lib.eqd_gpu_mlp_train.argtypes = [C.c_void_p, C.POINTER(MlpTrainOptions), f_p, f_p]
+        lib.eqd_gpu_mlp_get.argtypes = [C.c_void_p, f_p, f_p]
+        lib.eqd_gpu_mlp_set.argtypes = [C.c_void_p, f_p, f_p]
+        lib.eqd_gpu_mlp_enable.argtypes = [C.c_void_p, C.c_int32]
+        lib.eqd_gpu_newton_replay.argtypes = [C.c_void_p, C.c_int32, C.c_int32, i64_p, d_p]
+        lib.eqd_mlp_gradient.argtypes = [C.c_int32, f_p, f_p, f_p, C.c_int32, f_p, f_p]
+        for name in ("eqd_gpu_newton_log", "eqd_gpu_newton_records", "eqd_gpu_mlp_train", "eqd_gpu_mlp_get",
+                     "eqd_gpu_mlp_set", "eqd_gpu_mlp_enable", "eqd_gpu_newton_replay", "eqd_mlp_gradient"):
+            getattr(lib, name).restype = C.c_int
+        lib.eqd_gpu_newton_counts.argtypes = [C.c_void_p, C.POINTER(C.c_int64)]
+        lib.eqd_gpu_newton_counts.restype = C.c_int
         lib.eqd_gpu_table_info.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_int64)]
         lib.eqd_gpu_table_info.restype = C.c_int
         lib.eqd_gpu_fp64_fma_peak.argtypes = [C.c_int32, C.POINTER(C.c_double)]
@@ -162,7 +185,9 @@ def gpu_lib():
 # Entry points the C ABI must export (checked by the CPU test suite).
 GPU_SYMBOLS = ["eqd_gpu_init", "eqd_gpu_step", "eqd_gpu_fetch", "eqd_gpu_fetch_fault",
                "eqd_gpu_finalize", "eqd_gpu_status_string", "eqd_gpu_stats", "eqd_gpu_time",
-               "eqd_gpu_profile", "eqd_gpu_kernel_time", "eqd_gpu_table_info",
+               "eqd_gpu_profile", "eqd_gpu_kernel_time", "eqd_gpu_newton_counts", "eqd_gpu_table_info",
+               "eqd_gpu_newton_log", "eqd_gpu_newton_records", "eqd_gpu_mlp_train", "eqd_gpu_mlp_get",
+               "eqd_gpu_mlp_set", "eqd_gpu_mlp_enable", "eqd_gpu_newton_replay", "eqd_mlp_gradient",
                "eqd_gpu_fp64_fma_peak"]
 CASE_SYMBOLS = ["eqd_case_build", "eqd_case_view", "eqd_case_array_len", "eqd_case_dims",
                 "eqd_case_lines", "eqd_case_free", "eqd_case_last_error"]

@@ -1113,6 +1113,100 @@ int eqd_gpu_kernel_time(eqd_context *X, int32_t kind, double *ms, int64_t *launc
   return EQD_OK;
 }
 
+namespace {
+void drop_graph(Context &c) {  // a captured graph holds the fault kernel's arguments by value
+  if (c.graph) {
+    cudaGraphExecDestroy(c.graph);
+    c.graph = nullptr;
+  }
+}
+}  // namespace
+
+int eqd_gpu_newton_log(eqd_context *X, int32_t nsteps, int32_t stride) {
+  if (!X) return EQD_ERR_STATE;
+  Context &c = X->c;
+  cudaSetDevice(c.device);
+  EQD_CUDA_OK(cudaStreamSynchronize(c.stream));
+  drop_graph(c);
+  return newton_log_start(c, nsteps, stride);
+}
+
+int eqd_gpu_newton_records(eqd_context *X, double *host, int64_t cap, int64_t *count) {
+  if (!X) return EQD_ERR_STATE;
+  Context &c = X->c;
+  cudaSetDevice(c.device);
+  EQD_CUDA_OK(cudaStreamSynchronize(c.stream));
+  long long n = 0;
+  const int rc = newton_records(c, host, cap, &n);
+  if (count) *count = n;
+  return rc;
+}
+
+int eqd_gpu_mlp_train(eqd_context *X, const eqd_mlp_train_options *opt, float *epoch_loss, float *holdout_loss) {
+  if (!X) return EQD_ERR_STATE;
+  if (!opt) return EQD_ERR_INPUT;
+  Context &c = X->c;
+  cudaSetDevice(c.device);
+  EQD_CUDA_OK(cudaStreamSynchronize(c.stream));
+  drop_graph(c);
+  RC(mlp_train(c, *opt, epoch_loss, holdout_loss));
+  c.mlp_on = 1;
+  return EQD_OK;
+}
+
+int eqd_gpu_mlp_get(eqd_context *X, float *params, float *norm) {
+  if (!X) return EQD_ERR_STATE;
+  cudaSetDevice(X->c.device);
+  return mlp_get(X->c, params, norm);
+}
+
+int eqd_gpu_mlp_set(eqd_context *X, const float *params, const float *norm) {
+  if (!X) return EQD_ERR_STATE;
+  if (!params || !norm) return EQD_ERR_INPUT;
+  Context &c = X->c;
+  cudaSetDevice(c.device);
+  EQD_CUDA_OK(cudaStreamSynchronize(c.stream));
+  drop_graph(c);
+  RC(mlp_set(c, params, norm));
+  c.mlp_on = 1;
+  return EQD_OK;
+}
+
+int eqd_gpu_mlp_enable(eqd_context *X, int32_t on) {
+  if (!X) return EQD_ERR_STATE;
+  Context &c = X->c;
+  if (on && !c.mlp) return EQD_ERR_STATE;
+  cudaSetDevice(c.device);
+  EQD_CUDA_OK(cudaStreamSynchronize(c.stream));
+  drop_graph(c);
+  c.mlp_on = on ? 1 : 0;
+  return EQD_OK;
+}
+
+int eqd_gpu_newton_replay(eqd_context *X, int32_t learned, int32_t shortcut, int64_t counts[4], double *v_host) {
+  if (!X) return EQD_ERR_STATE;
+  if (!counts) return EQD_ERR_INPUT;
+  Context &c = X->c;
+  cudaSetDevice(c.device);
+  EQD_CUDA_OK(cudaStreamSynchronize(c.stream));
+  long long cc[4] = {0, 0, 0, 0};
+  RC(newton_replay(c, learned, shortcut, cc, v_host));
+  for (int k = 0; k < 4; ++k) counts[k] = cc[k];
+  return EQD_OK;
+}
+
+int eqd_gpu_newton_counts(eqd_context *X, int64_t out[4]) {
+  if (!X) return EQD_ERR_STATE;
+  if (!out) return EQD_ERR_INPUT;
+  Context &c = X->c;
+  unsigned long long st[4] = {0, 0, 0, 0};
+  cudaSetDevice(c.device);
+  EQD_CUDA_OK(cudaStreamSynchronize(c.stream));
+  EQD_CUDA_OK(cudaMemcpy(st, c.d_stats, sizeof(st), cudaMemcpyDeviceToHost));
+  for (int k = 0; k < 4; ++k) out[k] = (int64_t)st[k];
+  return EQD_OK;
+}
+
 int eqd_gpu_table_info(eqd_context *X, int32_t group, int64_t info[4]) {
   if (!X) return EQD_ERR_STATE;
   if ((group != 0 && group != 1) || !info) return EQD_ERR_INPUT;

@@ -113,12 +113,21 @@ struct Context {
   int *off_rows = nullptr;      // [3][nOffRows]: device node, component (0-2), type (1,2,3)
   double *offhist = nullptr;    // (nOffRows + 1, nstep)
   // MLP initial guess (rate-and-state)
-  void *mlp = nullptr;
+  void *mlp = nullptr;           // MlpDevice (device); used by the fault kernel while mlp_on
+  int mlp_on = 0;
+  float *mlp_p = nullptr;        // FP32 master parameters, gradients, Adam moments [kMlpParams]
+  float *mlp_g = nullptr, *mlp_m = nullptr, *mlp_v = nullptr;
+  float mlp_norm[18] = {};       // in_shift[8], in_scale[8], out_shift, out_scale
+  long long mlp_steps = 0;       // Adam steps taken
+  // logged rate-and-state Newton solves (training data of the learned guess)
+  double *nlog = nullptr;        // [nlog_steps][npair][16]
+  int nlog_nt0 = 0, nlog_steps = 0, nlog_stride = 1;
   // step bookkeeping
   int *d_nt = nullptr;          // current step index on the device
   double *d_times = nullptr;    // [nstep + 2] timeElapsed after nt steps
   int *d_err = nullptr;         // error word: 1 = NaN velocity, 2 = bounded wait gave up
-  unsigned long long *d_stats = nullptr;  // [4]: newton iterations, ivmax hits, ...
+  unsigned long long *d_stats = nullptr;  // [4]: Newton iterations (as counted by the reference),
+                                          // ivmax hits, iterations executed, learned guesses used
   int nt = 0;                   // steps completed (host mirror)
   double time = 0.0;
   int f_is_acc = 0;             // first node update consumes acceleration (from init state)
@@ -143,5 +152,12 @@ int launch_elements(Context &c, cudaStream_t s, int part = 2);  // 0 interior, 1
 int launch_fault(Context &c, cudaStream_t s);
 int mlp_init(Context &c);
 void mlp_free(Context &c);
+int newton_log_start(Context &c, int nsteps, int stride);
+long long newton_log_count(const Context &c);
+int newton_records(Context &c, double *host, long long cap, long long *count);
+int mlp_train(Context &c, const eqd_mlp_train_options &o, float *epoch_loss, float *holdout_loss);
+int mlp_get(Context &c, float *params, float *norm);
+int mlp_set(Context &c, const float *params, const float *norm);
+int newton_replay(Context &c, int learned, int shortcut, long long counts[4], double *v_host);
 
 }  // namespace eqd

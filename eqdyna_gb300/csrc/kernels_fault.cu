@@ -9,6 +9,7 @@
 //                (src/faulting.f90:518-541, src/driver.f90:157-180) and rupture time.
 #include "eqd_device.cuh"
 #include "mlp_common.cuh"
+#include "rsf_newton.cuh"
 
 namespace eqd {
 
@@ -93,6 +94,7 @@ __global__ void __launch_bounds__(kBlockNode)
 // tile); acceleration, its increment a*dt and the PML split-field velocities are binary32, while
 // velocity and displacement of every node stay binary64 (increments are small against the state,
 // which is accumulated over 10^3 - 10^4 steps).  About 6 binary64 operations per component.
+// Split (fault) nodes are updated entirely in binary64.
 template <bool F_IS_ACC>
 __global__ void __launch_bounds__(kBlockNode)
     node_update32(double *__restrict__ vel, double *__restrict__ disp, float *__restrict__ F,
@@ -203,34 +205,9 @@ struct FaultArgs {
   const double *d_times;
   unsigned long long *stats;
   const MlpDevice *mlp;       // learned initial guess, or null
+  double *newton_log;         // [log_steps][npair][kNewtonRecord] logged solves, or null
+  int log_nt0, log_steps, log_stride;  // steps log_nt0 + k log_stride, k = 1 .. log_steps
 };
-
-__device__ __forceinline__ void rsf_law(int friclaw, double V2, double &state, const double *fr,
-                                        int np, double dt, double &xmu, double &dxmudv) {
-  // fr(k) == fric(k) of this pair; src/fric.f90:39-95
-#define FR(k) fr[((k)-1) * np]
-  const double A = FR(9), B = FR(10), L = FR(11), f0 = FR(13), V0 = FR(12);
-  if (friclaw == 3) {
-    const double tmpc = 1.0 / (2.0 * V0) * exp((f0 + B * log(V0 * state / L)) / A);
-    const double tmp = (V2 + 1.e-30) * tmpc;
-    xmu = A * log(tmp + sqrt(tmp * tmp + 1.0));
-    dxmudv = A * tmpc / sqrt(1.0 + tmp * tmp);
-    state = L / V2 + (state - L / V2) * exp(-V2 * dt / L);
-  } else {
-    const double fw = FR(14), Vw = FR(15);
-    const double tmpc = 1.0 / (2.0 * V0) * exp(state / A);
-    const double tmp = (V2 + 1.e-30) * tmpc;
-    xmu = A * log(tmp + sqrt(tmp * tmp + 1.0));
-    dxmudv = A * tmpc / sqrt(1.0 + tmp * tmp);
-    const double fLV = f0 - (B - A) * log(V2 / V0);
-    const double r = V2 / Vw, r2 = r * r, r4 = r2 * r2;
-    const double fss = fw + (fLV - fw) / pow(1.0 + r4 * r4, 0.125);
-    const double fssa = fss / A;
-    const double psiss = A * log(2.0 * V0 / V2 * (exp(fssa) - exp(-fssa)) / 2.0);
-    state = psiss + (state - psiss) * exp(-V2 * dt / L);
-  }
-#undef FR
-}
 
 // Force of node `node`, component c, in the form's own precision.
 template <bool F32>
@@ -247,6 +224,7 @@ __device__ __forceinline__ void force_set(const FaultArgs &p, int c, int node, i
 
 template <bool F32>
 __global__ void __launch_bounds__(kBlockFault) fault_kernel(FaultArgs p) {
+  __shared__ __align__(16) __nv_bfloat16 mlp_xs[kBlockFault / 32][32 * kMlpK1];
   const int nt = *p.d_nt;
   const double t = p.d_times[nt];
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
@@ -359,7 +337,7 @@ __global__ void __launch_bounds__(kBlockFault) fault_kernel(FaultArgs p) {
   }
   tr[3] = sqrt(tr[1] * tr[1] + tr[2] * tr[2]);
 
-  unsigned iters = 0, maxhit = 0;
+  unsigned iters = 0, maxhit = 0, executed = 0, learned = 0;
   if (p.friclaw <= 2) {
     // solveSWTW (src/faulting.f90:136-188)
     double mu;
@@ -427,10 +405,11 @@ __global__ void __launch_bounds__(kBlockFault) fault_kernel(FaultArgs p) {
       FR(24) = thdot;
     }
     const double state0 = FR(20);
+    const RsfParams rp{FR(9), FR(10), FR(11), FR(12), FR(13), FR(14), FR(15)};
     double xmu, dxmudv;
     {
       double st = FR(20);
-      rsf_law(p.friclaw, vt, st, fr, np, dt, xmu, dxmudv);
+      rsf_law(p.friclaw, vt, st, rp, dt, xmu, dxmudv);
       FR(20) = st;
     }
     const double taoc_old = (p.friclaw == 5) ? FR(4) - xmu * tr[0] : xmu * thpc0;
@@ -440,37 +419,31 @@ __global__ void __launch_bounds__(kBlockFault) fault_kernel(FaultArgs p) {
 #pragma unroll
     for (int j = 1; j <= 2; ++j) trial[j] = tr[j] - taoc_old * 0.5 * (rate[j] / rate[3]) + FR(25 + j) / Tc;
     trial[3] = sqrt(trial[1] * trial[1] + trial[2] * trial[2]);
-    // learned initial guess for the Newton iteration (same residual, same exit test)
+    const NewtonSolve ns{rp, state0, thpc0, tr[0], trial[3], Tc, FR(4)};
+    // learned initial guess for the Newton iteration (same residual, same exit test): the
+    // tensor-core MLP over the warp's 32 pairs (the scalar path in the last, incomplete warp)
+    double v0 = vt;
     if (p.mlp) {
-      const double feat[6] = {log(vt), state0, tr[0], trial[3], FR(9), FR(10)};
-      const double g = mlp_guess(*p.mlp, feat);
-      if (g > 0.0 && isfinite(g)) vt = g;
+      float f[kMlpIn];
+      mlp_features(vt, state0, tr[0], trial[3], rp.A, rp.B, f);
+      const bool full = (tid & ~31) + 32 <= np;
+      v0 = mlp_guess_warp(*p.mlp, f, vt, full, mlp_xs[threadIdx.x >> 5]);
+      learned = 1;
     }
-    // NewtonRaphson (src/faulting.f90:459-516)
-    double stateTmp = state0, thTmp = thpc0, taoc_new = 0.0;
-    int iv;
-    for (iv = 1; iv <= 20; ++iv) {
-      stateTmp = state0;
-      rsf_law(p.friclaw, vt, stateTmp, fr, np, dt, xmu, dxmudv);
-      double rsfeq, dr;
-      if (p.friclaw < 5) {
-        thTmp = thpc0;
-        const double thdot = -vt / L * (thTmp - fabs(tr[0]));
-        thTmp = thTmp + thdot * dt;
-        taoc_new = xmu * thTmp;
-        rsfeq = vt + Tc * (taoc_new * 0.5 - trial[3]);
-        dr = 1.0 + Tc * (dxmudv * thTmp) * 0.5;
-      } else {
-        taoc_new = FR(4) - xmu * fmin(tr[0], 0.0);
-        rsfeq = vt + Tc * (taoc_new * 0.5 - trial[3]);
-        dr = 1.0 + Tc * (-dxmudv * fmin(tr[0], 0.0)) * 0.5;
-      }
-      if (fabs(rsfeq / dr) < 1.e-14 * fabs(vt) && fabs(rsfeq) < 1.e-6 * fabs(vt)) break;
-      const double vn = vt - rsfeq / dr;
-      vt = (vn <= 0.0) ? vt / 2.0 : vn;
+    const NewtonOut no = rsf_newton<true>(p.friclaw, dt, ns, v0);
+    const int lstep = nt - p.log_nt0;
+    if (p.newton_log && lstep > 0 && lstep % p.log_stride == 0 && lstep / p.log_stride <= p.log_steps) {
+      double *rec = p.newton_log + (size_t)kNewtonRecord * ((size_t)(lstep / p.log_stride - 1) * np + i);
+      const double vals[kNewtonRecord] = {rp.A,  rp.B,     rp.L,  rp.V0,    rp.f0,    rp.fw, rp.Vw, state0,
+                                          thpc0, tr[0],    trial[3], Tc, FR(4), vt,    no.v,  (double)no.iters};
+#pragma unroll
+      for (int k = 0; k < kNewtonRecord; ++k) rec[k] = vals[k];
     }
-    iters = iv > 20 ? 20 : iv;
-    maxhit = iv > 20 ? 1 : 0;
+    vt = no.v;
+    const double stateTmp = no.state, thTmp = no.th, taoc_new = no.taoc;
+    iters = no.iters;
+    maxhit = no.capped;
+    executed = no.executed;
     if (p.TPV == 105 && vt < FR(46)) vt = FR(46);
     FR(20) = stateTmp;
     FR(23) = thTmp;
@@ -501,6 +474,8 @@ __global__ void __launch_bounds__(kBlockFault) fault_kernel(FaultArgs p) {
   if (p.friclaw >= 3) {
     warp_count_add(p.stats + 0, iters);
     warp_count_add(p.stats + 1, maxhit);
+    warp_count_add(p.stats + 2, executed);
+    warp_count_add(p.stats + 3, learned);
   }
   // storeOnFaultStationQuantSCEC
   if (nt >= 1 && nt <= p.nstep) {
@@ -588,6 +563,10 @@ int launch_fault(Context &c, cudaStream_t s) {
   p.d_times = c.d_times;
   p.stats = c.d_stats;
   p.mlp = static_cast<const MlpDevice *>(mlp_device_params(c));
+  p.newton_log = c.nlog;
+  p.log_nt0 = c.nlog_nt0;
+  p.log_steps = c.nlog_steps;
+  p.log_stride = c.nlog_stride;
   const int grid = (nthreads + kBlockFault - 1) / kBlockFault;
   if (c.fp32) fault_kernel<true><<<grid, kBlockFault, 0, s>>>(p);
   else fault_kernel<false><<<grid, kBlockFault, 0, s>>>(p);

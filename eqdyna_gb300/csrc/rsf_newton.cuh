@@ -1,0 +1,121 @@
+// Rate-and-state friction law and the per-pair Newton solve for the slip rate
+// (src/fric.f90:39-95, src/faulting.f90:459-516), shared by the fault kernel and the kernel that
+// replays logged solves.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace eqd {
+
+// fric(9..15) of one pair: a, b, L, V0, f0, fw, Vw
+struct RsfParams {
+  double A, B, L, V0, f0, fw, Vw;
+};
+
+// Inputs of one Newton solve: the law's parameters, state and fric(23) before the solve, the
+// effective normal traction, the trial shear traction, Tc = area dt / reduced mass, fric(4).
+struct NewtonSolve {
+  RsfParams r;
+  double state0, th0, tn, trial, Tc, c0;
+};
+
+struct NewtonOut {
+  double v, state, th, taoc;
+  int iters;     // as the reference counts them (20 when the cap is reached)
+  int capped;    // 1 when the 20 iterations ran out without meeting the tolerance
+  int executed;  // iterations actually evaluated
+};
+
+// Logged solve: NewtonSolve (13 doubles), the plain initial guess, the converged slip rate and
+// the reference iteration count.
+constexpr int kNewtonRecord = 16;
+
+__device__ __forceinline__ void rsf_law(int friclaw, double V2, double &state, const RsfParams &p, double dt,
+                                        double &xmu, double &dxmudv) {
+  if (friclaw == 3) {  // aging law
+    const double tmpc = 1.0 / (2.0 * p.V0) * exp((p.f0 + p.B * log(p.V0 * state / p.L)) / p.A);
+    const double tmp = (V2 + 1.e-30) * tmpc;
+    xmu = p.A * log(tmp + sqrt(tmp * tmp + 1.0));
+    dxmudv = p.A * tmpc / sqrt(1.0 + tmp * tmp);
+    state = p.L / V2 + (state - p.L / V2) * exp(-V2 * dt / p.L);
+  } else {  // slip law with strong rate weakening
+    const double tmpc = 1.0 / (2.0 * p.V0) * exp(state / p.A);
+    const double tmp = (V2 + 1.e-30) * tmpc;
+    xmu = p.A * log(tmp + sqrt(tmp * tmp + 1.0));
+    dxmudv = p.A * tmpc / sqrt(1.0 + tmp * tmp);
+    const double fLV = p.f0 - (p.B - p.A) * log(V2 / p.V0);
+    const double r = V2 / p.Vw, r2 = r * r, r4 = r2 * r2;
+    const double fss = p.fw + (fLV - p.fw) / pow(1.0 + r4 * r4, 0.125);
+    const double fssa = fss / p.A;
+    const double psiss = p.A * log(2.0 * p.V0 / V2 * (exp(fssa) - exp(-fssa)) / 2.0);
+    state = psiss + (state - psiss) * exp(-V2 * dt / p.L);
+  }
+}
+
+// NewtonRaphson, at most 20 iterations from v0.  Iteration k evaluates the law at v_(k-1) and
+// forms v_k = f(v_(k-1)), a deterministic map; after 20 iterations the outputs are v_20 and the
+// law evaluated at v_19.  With SHORTCUT, when an iterate repeats (a fixed point v_k = v_(k-1), or
+// a 2-cycle v_k = v_(k-2): common for creeping nodes, whose residual cannot reach the tolerance in
+// binary64) every later iteration is known and the loop stops with the values iteration 20 would
+// give, bit for bit.
+template <bool SHORTCUT>
+__device__ __forceinline__ NewtonOut rsf_newton(int friclaw, double dt, const NewtonSolve &s, double v0) {
+  double vt = v0;
+  double stateTmp = s.state0, thTmp = s.th0, taoc_new = 0.0;
+  double vA = 0.0, stA = 0.0, thA = 0.0, tcA = 0.0;  // v_(k-2) and the law evaluated at it
+  int iv, executed = 0;
+  for (iv = 1; iv <= 20; ++iv) {
+    ++executed;
+    stateTmp = s.state0;
+    double xmu, dxmudv;
+    rsf_law(friclaw, vt, stateTmp, s.r, dt, xmu, dxmudv);
+    double rsfeq, dr;
+    if (friclaw < 5) {
+      thTmp = s.th0;
+      const double thdot = -vt / s.r.L * (thTmp - fabs(s.tn));
+      thTmp = thTmp + thdot * dt;
+      taoc_new = xmu * thTmp;
+      rsfeq = vt + s.Tc * (taoc_new * 0.5 - s.trial);
+      dr = 1.0 + s.Tc * (dxmudv * thTmp) * 0.5;
+    } else {
+      taoc_new = s.c0 - xmu * fmin(s.tn, 0.0);
+      rsfeq = vt + s.Tc * (taoc_new * 0.5 - s.trial);
+      dr = 1.0 + s.Tc * (-dxmudv * fmin(s.tn, 0.0)) * 0.5;
+    }
+    if (fabs(rsfeq / dr) < 1.e-14 * fabs(vt) && fabs(rsfeq) < 1.e-6 * fabs(vt)) break;
+    const double vn = vt - rsfeq / dr;
+    const double vnew = (vn <= 0.0) ? vt / 2.0 : vn;
+    if (SHORTCUT && iv < 20) {
+      if (vnew == vt) {  // fixed point: v_20 = v_19 = vt
+        iv = 21;
+        break;
+      }
+      if (iv >= 2 && vnew == vA) {  // 2-cycle vA, vt, vA, ...
+        if ((20 - iv) % 2 == 0) {
+          vt = vnew;  // v_20 = vA, v_19 = vt: the evaluation just made
+        } else {      // v_20 = vt, v_19 = vA: the previous evaluation
+          stateTmp = stA;
+          thTmp = thA;
+          taoc_new = tcA;
+        }
+        iv = 21;
+        break;
+      }
+    }
+    vA = vt;
+    stA = stateTmp;
+    thA = thTmp;
+    tcA = taoc_new;
+    vt = vnew;
+  }
+  NewtonOut o;
+  o.v = vt;
+  o.state = stateTmp;
+  o.th = thTmp;
+  o.taoc = taoc_new;
+  o.iters = iv > 20 ? 20 : iv;
+  o.capped = iv > 20 ? 1 : 0;
+  o.executed = executed;
+  return o;
+}
+
+}  // namespace eqd

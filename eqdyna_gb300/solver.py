@@ -85,6 +85,74 @@ class GpuSolver:
             out[name] = (ms.value, n.value)
         return out
 
+    def newton_counts(self):
+        """Rate-and-state Newton counters since init: iterations as the reference counts them,
+        solves that hit the 20-iteration cap, iterations executed, learned guesses used."""
+        out = (C.c_int64 * 4)()
+        rc = self.lib.eqd_gpu_newton_counts(self._h, out)
+        if rc != 0:
+            raise N.EqdError(rc, "eqd_gpu_newton_counts")
+        return dict(zip(["iterations", "ivmax_hits", "executed", "learned"], list(out)))
+
+    # ---- learned Newton initial guess ----
+    def newton_log(self, nsteps, stride=1):
+        """Log the rate-and-state Newton solves of the next nsteps * stride steps (one in stride)."""
+        self._rc(self.lib.eqd_gpu_newton_log(self._h, int(nsteps), int(stride)), "eqd_gpu_newton_log")
+
+    def newton_records(self):
+        """Logged solves as an array [n][16] (column meaning: EQD_NEWTON_RECORD)."""
+        n = C.c_int64()
+        self._rc(self.lib.eqd_gpu_newton_records(self._h, None, 0, C.byref(n)), "eqd_gpu_newton_records")
+        buf = np.zeros((n.value, N.NEWTON_RECORD))
+        self._rc(self.lib.eqd_gpu_newton_records(self._h, buf.ctypes.data_as(N.c_double_p), n.value, C.byref(n)),
+                 "eqd_gpu_newton_records")
+        return buf
+
+    def train_mlp(self, epochs=8, batch=4096, lr=1e-3, holdout=0.05, seed=20261203):
+        """Train the guess on the logged solves and enable it; returns the loss history."""
+        opt = N.MlpTrainOptions(int(epochs), int(batch), float(lr), float(holdout), int(seed))
+        el = np.zeros(max(int(epochs), 1), dtype=np.float32)
+        hl = C.c_float()
+        self._rc(self.lib.eqd_gpu_mlp_train(self._h, C.byref(opt), el.ctypes.data_as(C.POINTER(C.c_float)),
+                                            C.byref(hl)), "eqd_gpu_mlp_train")
+        return {"epoch_loss": el[: int(epochs)].tolist(), "holdout_loss": hl.value}
+
+    def mlp_state(self):
+        params = np.zeros(N.MLP_PARAMS, dtype=np.float32)
+        norm = np.zeros(N.MLP_NORM, dtype=np.float32)
+        self._rc(self.lib.eqd_gpu_mlp_get(self._h, params.ctypes.data_as(C.POINTER(C.c_float)),
+                                          norm.ctypes.data_as(C.POINTER(C.c_float))), "eqd_gpu_mlp_get")
+        return params, norm
+
+    def set_mlp(self, params, norm):
+        params = np.ascontiguousarray(params, dtype=np.float32)
+        norm = np.ascontiguousarray(norm, dtype=np.float32)
+        self._rc(self.lib.eqd_gpu_mlp_set(self._h, params.ctypes.data_as(C.POINTER(C.c_float)),
+                                          norm.ctypes.data_as(C.POINTER(C.c_float))), "eqd_gpu_mlp_set")
+
+    def enable_mlp(self, on=True):
+        self._rc(self.lib.eqd_gpu_mlp_enable(self._h, int(bool(on))), "eqd_gpu_mlp_enable")
+
+    def replay(self, learned=False, shortcut=True, values=False):
+        """Re-solve the logged records: counts (+ converged slip rates when values=True)."""
+        counts = (C.c_int64 * 4)()
+        v = None
+        vp = None
+        if values:
+            n = C.c_int64()
+            self._rc(self.lib.eqd_gpu_newton_records(self._h, None, 0, C.byref(n)), "eqd_gpu_newton_records")
+            v = np.zeros(n.value)
+            vp = v.ctypes.data_as(N.c_double_p)
+        self._rc(self.lib.eqd_gpu_newton_replay(self._h, int(bool(learned)), int(bool(shortcut)), counts, vp),
+                 "eqd_gpu_newton_replay")
+        out = dict(zip(["iterations", "ivmax_hits", "executed", "records"], list(counts)))
+        return (out, v) if values else out
+
+    @staticmethod
+    def _rc(rc, what):
+        if rc != 0:
+            raise N.EqdError(rc, what)
+
     def table_info(self):
         """Binary32 element-table layout per group: {"interior"|"pml": {layout, elements, records,
         record_floats}}; layout is "records", "streamed" or None (empty group / binary64 form)."""
@@ -118,3 +186,20 @@ class GpuSolver:
             self.close()
         except Exception:
             pass
+
+
+def mlp_gradient(params, x, t, device=0):
+    """Loss sum((y - t)^2) / (2 n) and its gradient computed by the tensor-core training kernel
+    (x: [n][6] normalised inputs, t: [n] normalised targets)."""
+    lib = N.gpu_lib()
+    params = np.ascontiguousarray(params, dtype=np.float32)
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    t = np.ascontiguousarray(t, dtype=np.float32)
+    loss = C.c_float()
+    grad = np.zeros(N.MLP_PARAMS, dtype=np.float32)
+    fp = C.POINTER(C.c_float)
+    rc = lib.eqd_mlp_gradient(int(device), params.ctypes.data_as(fp), x.ctypes.data_as(fp), t.ctypes.data_as(fp),
+                              int(len(t)), C.byref(loss), grad.ctypes.data_as(fp))
+    if rc != 0:
+        raise N.EqdError(rc, "eqd_mlp_gradient")
+    return loss.value, grad

@@ -109,8 +109,9 @@ typedef struct eqd_host_arrays {
 /* ---- precision / solver options of the GPU form ------------------------------------------- */
 enum eqd_precision {
   EQD_PREC_FP64 = 0,      /* plain form: every operation in binary64 (the drop-in)             */
-  EQD_PREC_FP32 = 1       /* element strain/stress/hourglass in binary32 with compensated
-                             binary32 nodal accumulation; state, fault and Newton in binary64  */
+  EQD_PREC_FP32 = 1       /* element strain/stress/hourglass in binary32 with Kahan-compensated
+                             binary32 nodal sums and PML split fields; velocity/displacement
+                             state, fault and Newton in binary64                               */
 };
 
 /* Element-table layout of the binary32 form (results are identical in both layouts). */
@@ -174,6 +175,55 @@ int eqd_gpu_profile(eqd_context *ctx, int32_t enable);
 /* Milliseconds and launch count accumulated while profiling, per kind:
  * 0 whole steps, 1 node update, 2 interior elements, 3 PML elements, 4 fault + stations. */
 int eqd_gpu_kernel_time(eqd_context *ctx, int32_t kind, double *ms, int64_t *launches);
+
+/* Rate-and-state Newton counters summed over pairs and steps since init: out[0] iterations as
+ * the reference counts them (src/faulting.f90:459-516, at most 20 per solve), out[1] solves that
+ * reached 20, out[2] iterations executed (the loop stops early, with identical results, once an
+ * iterate repeats), out[3] solves that started from the learned initial guess. */
+int eqd_gpu_newton_counts(eqd_context *ctx, int64_t out[4]);
+
+/* ---- learned initial guess of the rate-and-state Newton solve ------------------------------
+ * No counterpart in the reference.  A 6 -> 64 -> 64 -> 1 MLP (BF16 tensor cores, FP32
+ * accumulation) predicts ln(V / V_trial) of the converged slip rate from (ln V_trial, ln |state|,
+ * normal traction, trial shear traction, a, b); Newton then runs to the reference's own exit
+ * test from that guess.  It is trained on solves the plain method logs (friclaw 3 or 4). */
+#define EQD_NEWTON_RECORD 16  /* doubles per logged solve: a b L V0 f0 fw Vw state0 fric(23)
+                                 normal-traction trial-shear Tc fric(4) V_trial V iterations   */
+#define EQD_MLP_PARAMS 5313   /* FP32 parameters: W1[64][16] b1[64] W2[64][64] b2[64] W3[64] b3 */
+#define EQD_MLP_NORM 18       /* in_shift[8] in_scale[8] out_shift out_scale                     */
+
+typedef struct eqd_mlp_train_options {
+  int32_t epochs;         /* passes over the training records                                  */
+  int32_t batch;          /* records per Adam step (rounded up to a multiple of 64)            */
+  float lr;               /* Adam learning rate                                                */
+  float holdout;          /* fraction of the records held out for the reported holdout loss    */
+  uint64_t seed;          /* initial weights and shuffles                                      */
+} eqd_mlp_train_options;
+
+/* Logs every Newton solve of the next nsteps * stride steps, one step in `stride`, into a
+ * device buffer owned by the context (nsteps * npair records); nsteps = 0 drops the log. */
+int eqd_gpu_newton_log(eqd_context *ctx, int32_t nsteps, int32_t stride);
+/* Number of records logged so far and, when host != NULL, copies up to cap of them. */
+int eqd_gpu_newton_records(eqd_context *ctx, double *host, int64_t cap, int64_t *count);
+/* Trains the guess on the logged records and enables it for the following steps.
+ * epoch_loss[epochs] and holdout_loss may be NULL. */
+int eqd_gpu_mlp_train(eqd_context *ctx, const eqd_mlp_train_options *opt, float *epoch_loss,
+                      float *holdout_loss);
+/* FP32 parameters and normalisation of the current model (either may be NULL). */
+int eqd_gpu_mlp_get(eqd_context *ctx, float *params, float *norm);
+/* Loads a model (e.g. saved by eqd_gpu_mlp_get) and enables it. */
+int eqd_gpu_mlp_set(eqd_context *ctx, const float *params, const float *norm);
+/* on = 1 uses the loaded model as the Newton initial guess, on = 0 the plain one. */
+int eqd_gpu_mlp_enable(eqd_context *ctx, int32_t on);
+/* Re-solves every logged record from the plain (learned = 0) or learned initial guess, with or
+ * without the repeated-iterate shortcut: counts = {iterations as the reference counts them,
+ * solves that reached 20, iterations executed, records}; v_host[records] may be NULL. */
+int eqd_gpu_newton_replay(eqd_context *ctx, int32_t learned, int32_t shortcut, int64_t counts[4],
+                          double *v_host);
+/* Loss sum((y - t)^2) / (2 n) and its gradient for a model and a batch, computed by the training
+ * kernel: x[n][6] normalised inputs, t[n] normalised targets (gradient checks). */
+int eqd_mlp_gradient(int32_t device, const float *params, const float *x, const float *t, int32_t n,
+                     float *loss, float *grad);
 
 /* Element-table layout of the binary32 form for group 0 (interior) or 1 (PML):
  * info[0] = 2 record-indexed, 1 streamed, 0 group empty or binary64 form; info[1] = elements;

@@ -1,0 +1,99 @@
+"""Learned Newton initial guess and the logged-solve machinery.
+
+* the tensor-core training kernel's loss and gradient against the numpy reference (mlp_ref);
+* logged solves replay bit for bit, with and without the repeated-iterate shortcut, and the
+  shortcut keeps the reference's iteration count while executing fewer iterations;
+* training on solves logged by the plain method lowers the loss; iteration counts of the plain
+  and the learned guess are reported; every solve converges to the same slip rate from either
+  guess; the binary32 form with the learned guess stays within the accuracy budget.
+"""
+import tempfile
+
+import numpy as np
+import pytest
+
+from conftest import nthreads
+from mlp_ref import BLOCKS, NIN, he_params, loss_grad
+
+pytestmark = pytest.mark.gpu
+
+
+def test_mlp_gradient_matches_numpy_reference():
+    from eqdyna_gb300.solver import mlp_gradient
+    rng = np.random.default_rng(7)
+    p = he_params(rng)
+    x = rng.standard_normal((300, NIN)).astype(np.float32)
+    t = rng.standard_normal(300).astype(np.float32)
+    loss, g = mlp_gradient(p, x, t)
+    lr, gr = loss_grad(p, x, t, rounded=True)
+    print("loss", loss, lr)
+    assert abs(loss - lr) <= 1e-3 * lr
+    for name, sl in BLOCKS.items():
+        rel = np.linalg.norm(g[sl] - gr[sl]) / np.linalg.norm(gr[sl])
+        print(name, rel)
+        assert rel <= 1e-2, name
+
+
+@pytest.fixture(scope="module")
+def c1_logged():
+    """C1 at dx = 400 m, plain binary64 method, every other step of the first 160 logged."""
+    from eqdyna_gb300.case import Case
+    from eqdyna_gb300.configs import config_c1
+    from eqdyna_gb300.solver import GpuSolver
+    case = Case.from_dir(config_c1(tempfile.mkdtemp(prefix="eqd_c1_"), scale=4.0, nsteps=300))
+    s = GpuSolver(case.clone(), precision="fp64")
+    s.newton_log(80, stride=2)
+    s.step(160)
+    yield s, case
+    s.close()
+
+
+def test_logged_solves_replay_bit_for_bit(c1_logged):
+    s, case = c1_logged
+    rec = s.newton_records()
+    assert rec.shape == (80 * case.npair, 16)
+    full, v_full = s.replay(learned=False, shortcut=False, values=True)
+    short, v_short = s.replay(learned=False, shortcut=True, values=True)
+    print("all iterations", full, "shortcut", short)
+    assert np.array_equal(v_full, rec[:, 14])
+    assert np.array_equal(v_short, rec[:, 14])
+    assert full["iterations"] == short["iterations"] == int(rec[:, 15].sum())
+    assert full["executed"] == full["iterations"]
+    assert short["executed"] < full["executed"]
+
+
+def test_learned_guess_trains_and_converges_to_the_same_solutions(c1_logged):
+    s, _ = c1_logged
+    hist = s.train_mlp(epochs=20, batch=1024, lr=2e-3, holdout=0.1, seed=5)
+    print("loss", hist)
+    assert hist["epoch_loss"][-1] < 0.5 * hist["epoch_loss"][0]
+    assert hist["holdout_loss"] < 2.0 * hist["epoch_loss"][-1]
+    plain, vp = s.replay(learned=False, values=True)
+    learned, vl = s.replay(learned=True, values=True)
+    print("plain guess", plain, "learned guess", learned)
+    rel = np.abs(vl - vp) / np.abs(vp)
+    print("max relative difference of the converged slip rate", rel.max(), "median", np.median(rel))
+    assert np.quantile(rel, 0.999) <= 1e-9
+    s.enable_mlp(False)
+
+
+def test_fp32_learned_form_within_budget(c1_logged):
+    """The model trained on the plain solves drives the binary32 form over C1 (dx = 400 m, 300
+    steps) within the slip-rate budget of the binary64 oracle."""
+    from eqdyna_gb300.solver import GpuSolver
+    from oracle import Oracle
+    from test_gpu_fp32 import _check, _errors
+    s, case = c1_logged
+    params, norm = s.mlp_state()
+    cpu = case.clone()
+    Oracle(cpu, nthreads()).step(300)
+    gpu = case.clone()
+    with GpuSolver(gpu, precision="fp32") as g:
+        g.set_mlp(params, norm)
+        g.step(300)
+        g.fetch()
+        counts = g.newton_counts()
+    err = _errors(cpu, gpu)
+    print("fp32+learned", err, counts)
+    assert counts["learned"] == 300 * case.npair
+    _check(err)
