@@ -55,6 +55,16 @@ ELEM_BYTES = {"fp64": {"interior": 32 + 192 + 8 + 16 + 96 + 256 + 48,
               "fp32": {"interior": 16 + 96 + 4 + 8 + 48 + 128 + 24,
                        "pml": 16 + 96 + 4 + 8 + 120 + 128 + 24 + 24}}
 REC_ELEM_BYTES = {"interior": 16 + 4 + 48, "pml": 16 + 4 + 120 + 8}
+# Node update (per node): fp64 form 152 B (3-DOF) / 536 B (PML); fp32 form 148 B / 340 B
+# (binary64 velocity and displacement, binary32 forces, 1/m and PML split fields, plus the
+# binary32 copies the element kernels gather).
+NODE_BYTES = {"fp64": (152, 536), "fp32": (148, 340)}
+# DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) per element of the binary32
+# kernels on a uniform grid (one record per group), from the ncu capture of C1 at dx = 200 m
+# (profiles/elem_f32_uniform_C1-dx200.md), scaled to a launch by its element count.
+NCU_TRAFFIC_PER_UNIT = {("elem_interior", "records", 1): (105.420032e6 + 10.960384e6) / 1125000,
+                        ("elem_pml", "records", 1): (256.453376e6 + 106.076672e6) / 1402000}
+JOB_STEPS = {"C0": 1000, "C1": 4000}
 NODE_GATHER_BYTES = {"fp64": 48 + 24, "fp32": 24 + 12}
 PML_NODE_EXTRA = {"fp64": 72, "fp32": 36}
 FP64_FLOPS_PER_ELEM = {"interior": 2 * 423, "pml": 2 * 470}
@@ -150,6 +160,9 @@ def algorithmic_bytes(case, precision, tables=None):
         else:
             elem = ne * ELEM_BYTES[precision][name]
         out[name] = (elem + len(nodes) * NODE_GATHER_BYTES[precision] + npml_nodes * PML_NODE_EXTRA[precision], ne)
+    n12 = int((nd == 12).sum())
+    n3 = len(nd) - n12
+    out["node"] = (n3 * NODE_BYTES[precision][0] + n12 * NODE_BYTES[precision][1], len(nd))
     return out
 
 
@@ -248,38 +261,61 @@ def bench_ours(args, world, rank, local):
     lib = N.gpu_lib()
     t_setup = time.perf_counter()
     tmp = tempfile.mkdtemp(prefix="eqd_bench_")
-    total_steps = 2 * (args.steps + args.warmup) + 4 + (args.log_steps * args.log_stride if args.learned else 0)
+    job = args.job_steps if args.job_steps > 0 else JOB_STEPS[args.config]
+    total_steps = max(job, args.steps + args.warmup + 4)
     case = build_case(args.config, args.scale, total_steps, tmp)
     shutil.rmtree(tmp, ignore_errors=True)
     ne = case.sizes["nelem"]
     host_bytes_in = sum(v.nbytes for k, v in case.arrays.items() if v is not None)
     setup_s = time.perf_counter() - t_setup
-
     npair = case.npair
-    d2h_per_step = 100 * npair * 8 + npair * 8
+    d2h_per_step = (100 * npair + npair) * 8  # fric + fnft after every step
     args.learned = int(bool(args.learned) and case.scalars.friclaw in (3, 4))  # rate-and-state only
+    nlog = min(args.log_steps * args.log_stride, job) if args.learned else 0
+
+    # ---- end to end: the whole job through the C ABI with host buffers ----
+    e2e_case = case.clone()
+    fr = np.zeros_like(e2e_case.arrays["fric"])
+    fn = np.zeros_like(e2e_case.arrays["fnft"])
+    barrier(world)
+    t0 = time.perf_counter()
+    s = GpuSolver(e2e_case, precision=args.precision, learned_guess=args.learned, device=local,
+                  table_layout=args.tables)
+    done, train_s, hist = 0, 0.0, None
+    if args.learned:  # plain warm-up whose Newton solves are the training data, then training
+        s.newton_log(nlog // args.log_stride, args.log_stride)
+        for _ in range(nlog):
+            s.step(1)
+            s.fetch_fault(fr, fn)
+        done = nlog
+        t1 = time.perf_counter()
+        hist = s.train_mlp(epochs=args.epochs, batch=4096, lr=1e-3, holdout=0.05, seed=20261203)
+        train_s = time.perf_counter() - t1
+    for _ in range(job - done):
+        s.step(1)
+        s.fetch_fault(fr, fn)
+    s.fetch()
+    e2e_s = time.perf_counter() - t0
+    job_newton = s.newton_counts()
+    learned = None
+    if args.learned:
+        plain = s.replay(learned=False)
+        guess = s.replay(learned=True)
+        params, norm = s.mlp_state()
+        learned = {"records": plain["records"], "logged_steps": nlog // args.log_stride,
+                   "log_stride": args.log_stride, "train_s": round(train_s, 2), "epochs": args.epochs,
+                   "epoch_loss": [round(x, 5) for x in hist["epoch_loss"]],
+                   "holdout_loss": round(hist["holdout_loss"], 5),
+                   "replay_plain_guess": plain, "replay_learned_guess": guess, "job_newton": job_newton}
+    s.close()
+    e2e_s = allreduce_max(e2e_s, world)
+    del e2e_case
 
     # ---- device-timed steps (inputs resident in HBM) ----
     s = GpuSolver(case.clone(), precision=args.precision, learned_guess=args.learned, device=local,
                   table_layout=args.tables)
-    learned = None
     if args.learned:
-        # seeded warm-up of the plain method whose Newton solves are the training data
-        t0 = time.perf_counter()
-        s.newton_log(args.log_steps, args.log_stride)
-        s.step(args.log_steps * args.log_stride)
-        warm_s = time.perf_counter() - t0
-        t0 = time.perf_counter()
-        hist = s.train_mlp(epochs=args.epochs, batch=4096, lr=1e-3, holdout=0.05, seed=20261203)
-        train_s = time.perf_counter() - t0
-        plain = s.replay(learned=False)
-        guess = s.replay(learned=True)
-        params, norm = s.mlp_state()
-        learned = {"records": plain["records"], "warmup_steps": args.log_steps * args.log_stride,
-                   "log_stride": args.log_stride, "warmup_s": round(warm_s, 2), "train_s": round(train_s, 2),
-                   "epochs": args.epochs, "epoch_loss": [round(x, 5) for x in hist["epoch_loss"]],
-                   "holdout_loss": round(hist["holdout_loss"], 5),
-                   "replay_plain_guess": plain, "replay_learned_guess": guess}
+        s.set_mlp(params, norm)
     s.step(args.warmup)
     n_before = s.newton_counts()
     s.profile(True, reset=True)
@@ -301,46 +337,36 @@ def bench_ours(args, world, rank, local):
     value = units / dev_s
     s.close()
 
-    # ---- end to end through the C ABI with host buffers ----
-    e2e_case = case.clone()
-    fr = np.zeros_like(e2e_case.arrays["fric"])
-    fn = np.zeros_like(e2e_case.arrays["fnft"])
-    barrier(world)
-    t0 = time.perf_counter()
-    s = GpuSolver(e2e_case, precision=args.precision, learned_guess=args.learned, device=local,
-                  table_layout=args.tables)
-    if args.learned:
-        s.set_mlp(params, norm)
-    for _ in range(args.steps):
-        s.step(1)
-        s.fetch_fault(fr, fn)
-    s.fetch()
-    e2e_s = time.perf_counter() - t0
-    s.close()
-    e2e_s = allreduce_max(e2e_s, world)
-    del e2e_case
-
-    # ---- roofline of the dominant kernel ----
+    # ---- rooflines: every kernel, the one with the largest time share on top ----
     hbm_peak, peak_kind = _peaks()
     ab = algorithmic_bytes(case, args.precision, tables)
-    working_set = ab["interior"][0] + ab["pml"][0]
-    dom = "elem_interior" if kt["elem_interior"][0] >= kt["elem_pml"][0] else "elem_pml"
-    key = "interior" if dom == "elem_interior" else "pml"
-    ms, nl = kt[dom]
-    avg_s = ms / 1e3 / max(nl, 1)
-    bytes_per_launch = ab[key][0]
-    achieved = bytes_per_launch / avg_s / 1e9
-    roofline = {"bound": "hbm", "kernel": f"{dom}_{args.precision}", "achieved": achieved,
-                "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
-                "peak_source": peak_kind, "traffic": None,
-                "algorithmic_bytes_per_launch": bytes_per_launch, "elements_per_launch": ab[key][1],
-                "avg_launch_ms": avg_s * 1e3,
-                "kernel_share": {k: v[0] / step_ms_total for k, v in kt.items() if k != "step"}}
+    working_set = ab["interior"][0] + ab["pml"][0] + ab["node"][0]
+    per_kernel = {}
+    for kname, key in (("node_update", "node"), ("elem_interior", "interior"), ("elem_pml", "pml")):
+        ms, nl = kt[kname]
+        if nl == 0:
+            continue
+        avg_s = ms / 1e3 / nl
+        tkey = (kname, (tables.get(key) or {}).get("layout"), (tables.get(key) or {}).get("records"))
+        traffic = NCU_TRAFFIC_PER_UNIT.get(tkey) if args.precision == "fp32" else None
+        per_kernel[kname] = {"achieved": ab[key][0] / avg_s / 1e9, "frac": ab[key][0] / avg_s / 1e9 / hbm_peak,
+                             "algorithmic_bytes_per_launch": ab[key][0], "units_per_launch": ab[key][1],
+                             "avg_launch_ms": avg_s * 1e3, "share": ms / step_ms_total,
+                             "traffic": traffic * ab[key][1] if traffic else None}
+    dom = max(per_kernel, key=lambda k: per_kernel[k]["share"])
+    d = per_kernel[dom]
+    roofline = {"bound": "hbm", "kernel": f"{dom}_{args.precision}", "achieved": d["achieved"], "peak": hbm_peak,
+                "unit": "GB/s", "frac": d["frac"], "peak_source": peak_kind, "traffic": d["traffic"],
+                "algorithmic_bytes_per_launch": d["algorithmic_bytes_per_launch"],
+                "units_per_launch": d["units_per_launch"], "avg_launch_ms": d["avg_launch_ms"],
+                "kernels": per_kernel, "kernel_share": {k: v[0] / step_ms_total for k, v in kt.items() if k != "step"}}
     if args.precision == "fp64":
         fp64 = C.c_double()
-        if lib.eqd_gpu_fp64_fma_peak(local, C.byref(fp64)) == 0:
-            fl = FP64_FLOPS_PER_ELEM[key] * ab[key][1] / avg_s / 1e12
-            roofline["fp64"] = {"achieved_tflops": fl, "peak_tflops": fp64.value,
+        key = "interior" if kt["elem_interior"][0] >= kt["elem_pml"][0] else "pml"
+        ms, nl = kt["elem_" + key]
+        if lib.eqd_gpu_fp64_fma_peak(local, C.byref(fp64)) == 0 and nl:
+            fl = FP64_FLOPS_PER_ELEM[key] * ab[key][1] / (ms / 1e3 / nl) / 1e12
+            roofline["fp64"] = {"kernel": "elem_" + key, "achieved_tflops": fl, "peak_tflops": fp64.value,
                                 "frac": fl / fp64.value, "flops_per_element": FP64_FLOPS_PER_ELEM[key],
                                 "peak_source": "measured FMA-chain kernel"}
     cpu = run_cpu_baseline(case, args.cpu_seconds) if (rank == 0 and world == 1 and args.cpu_seconds > 0) else None
@@ -353,15 +379,18 @@ def bench_ours(args, world, rank, local):
             "config": {"workload": f"{args.config}: {WORKLOADS[args.config]}", "elements": ne,
                        "physical_elements": case.dims["n_phys_elem"], "precision": args.precision,
                        "learned_guess": bool(args.learned), "scale": args.scale,
-                       "l2": f"inputs larger than L2: element-kernel working set "
-                             f"{working_set / 1e9:.2f} GB per step vs 129 MB L2, no flush",
+                       "l2": f"inputs larger than L2: working set {working_set / 1e9:.2f} GB per step "
+                             "vs 129 MB L2, no flush",
                        "element_tables": {k: (v["layout"], v["records"]) for k, v in tables.items()},
                        "parallelism": "replicas" if world > 1 else "single GPU",
                        "setup_s": round(setup_s, 1), "wall_ms_per_step": wall * 1e3 / args.steps},
-            "e2e": {"value": units / e2e_s if world > 1 else ne * args.steps / e2e_s, "unit": UNIT,
-                    "h2d_bytes_per_step": int(host_bytes_in / args.steps),
-                    "d2h_bytes_per_step": int(d2h_per_step + host_bytes_in / args.steps),
-                    "note": "init (every table host->device) + per-step fault-state read + final fetch"},
+            "e2e": {"value": ne * job * world / e2e_s, "unit": UNIT, "steps": job,
+                    "h2d_bytes_per_step": int(host_bytes_in / job),
+                    "d2h_bytes_per_step": int(d2h_per_step + host_bytes_in / job),
+                    "note": "whole job through the C ABI: init (every host table to the device), each step "
+                            "followed by a read of the fault state (fric, fnft), final fetch of every array"
+                            + ("; the first steps run the plain Newton with solve logging, then training"
+                               if args.learned else "")},
             "gpu_launches": int(stats["kernel_launches"]),
             "newton": newton,
             "learned": learned,
@@ -383,6 +412,7 @@ def main():
     ap.add_argument("--log-steps", type=int, default=70, help="logged warm-up steps (training data)")
     ap.add_argument("--log-stride", type=int, default=10, help="one logged step in this many")
     ap.add_argument("--epochs", type=int, default=8)
+    ap.add_argument("--job-steps", type=int, default=0, help="steps of the end-to-end job (0: the config's)")
     ap.add_argument("--tables", default="auto", choices=["auto", "streamed", "records"],
                     help="binary32 element-table layout")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])

@@ -1183,14 +1183,14 @@ int eqd_gpu_mlp_enable(eqd_context *X, int32_t on) {
   return EQD_OK;
 }
 
-int eqd_gpu_newton_replay(eqd_context *X, int32_t learned, int32_t shortcut, int64_t counts[4], double *v_host) {
+int eqd_gpu_newton_replay(eqd_context *X, int32_t learned, int32_t fast, int64_t counts[4], double *v_host) {
   if (!X) return EQD_ERR_STATE;
   if (!counts) return EQD_ERR_INPUT;
   Context &c = X->c;
   cudaSetDevice(c.device);
   EQD_CUDA_OK(cudaStreamSynchronize(c.stream));
   long long cc[4] = {0, 0, 0, 0};
-  RC(newton_replay(c, learned, shortcut, cc, v_host));
+  RC(newton_replay(c, learned, fast, cc, v_host));
   for (int k = 0; k < 4; ++k) counts[k] = cc[k];
   return EQD_OK;
 }

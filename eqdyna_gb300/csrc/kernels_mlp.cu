@@ -294,7 +294,7 @@ constexpr size_t kGradSmem = (size_t)(kMlpH * kMlpK1 + 2 * kMlpH * kMlpH + kMlpN
 
 // Replays logged solves from the plain guess or the learned one; ghost lanes past n re-solve the
 // last record so every warp is complete for the tensor-core guess, and write nothing.
-template <bool SHORTCUT>
+template <bool FAST>
 __global__ void __launch_bounds__(128) newton_replay_kernel(const double *__restrict__ rec, long long n,
                                                             int friclaw, double dt, const MlpDevice *m,
                                                             double *__restrict__ v_out,
@@ -317,7 +317,7 @@ __global__ void __launch_bounds__(128) newton_replay_kernel(const double *__rest
     mlp_features(q[13], q[7], q[9], q[10], q[0], q[1], f);
     v0 = mlp_guess_warp(*m, f, q[13], true, xs[threadIdx.x >> 5]);
   }
-  const NewtonOut o = rsf_newton<SHORTCUT>(friclaw, dt, s, v0);
+  const NewtonOut o = rsf_newton<FAST>(friclaw, dt, s, v0);
   if (live) {
     if (v_out) v_out[i] = o.v;
     warp_count_add(counts + 0, (unsigned)o.iters);
@@ -543,7 +543,7 @@ int mlp_train(Context &c, const eqd_mlp_train_options &o, float *epoch_loss, flo
   return rc;
 }
 
-int newton_replay(Context &c, int learned, int shortcut, long long counts[4], double *v_host) {
+int newton_replay(Context &c, int learned, int fast, long long counts[4], double *v_host) {
   const long long n = newton_log_count(c);
   if (n <= 0) return EQD_ERR_STATE;
   if (learned && !c.mlp) return EQD_ERR_STATE;
@@ -558,7 +558,7 @@ int newton_replay(Context &c, int learned, int shortcut, long long counts[4], do
   }
   const unsigned grid = (unsigned)((n + 127) / 128);
   const MlpDevice *m = learned ? static_cast<const MlpDevice *>(c.mlp) : nullptr;
-  if (shortcut) newton_replay_kernel<true><<<grid, 128>>>(c.nlog, n, c.sc.friclaw, c.sc.dt, m, dv, dc);
+  if (fast) newton_replay_kernel<true><<<grid, 128>>>(c.nlog, n, c.sc.friclaw, c.sc.dt, m, dv, dc);
   else newton_replay_kernel<false><<<grid, 128>>>(c.nlog, n, c.sc.friclaw, c.sc.dt, m, dv, dc);
   unsigned long long h[4] = {0, 0, 0, 0};
   if (cudaMemcpy(h, dc, sizeof(h), cudaMemcpyDeviceToHost) != cudaSuccess) rc = EQD_ERR_CUDA;

@@ -51,27 +51,55 @@ __device__ __forceinline__ void rsf_law(int friclaw, double V2, double &state, c
   }
 }
 
+// State evolution of the law at slip rate V2 (the state half of rsf_law).
+__device__ __forceinline__ double rsf_state(int friclaw, double V2, double state, const RsfParams &p, double dt) {
+  if (friclaw == 3) return p.L / V2 + (state - p.L / V2) * exp(-V2 * dt / p.L);
+  const double fLV = p.f0 - (p.B - p.A) * log(V2 / p.V0);
+  const double r = V2 / p.Vw, r2 = r * r, r4 = r2 * r2;
+  const double fss = p.fw + (fLV - p.fw) / pow(1.0 + r4 * r4, 0.125);
+  const double fssa = fss / p.A;
+  const double psiss = p.A * log(2.0 * p.V0 / V2 * (exp(fssa) - exp(-fssa)) / 2.0);
+  return psiss + (state - psiss) * exp(-V2 * dt / p.L);
+}
+
 // NewtonRaphson, at most 20 iterations from v0.  Iteration k evaluates the law at v_(k-1) and
 // forms v_k = f(v_(k-1)), a deterministic map; after 20 iterations the outputs are v_20 and the
-// law evaluated at v_19.  With SHORTCUT, when an iterate repeats (a fixed point v_k = v_(k-1), or
-// a 2-cycle v_k = v_(k-2): common for creeping nodes, whose residual cannot reach the tolerance in
-// binary64) every later iteration is known and the loop stops with the values iteration 20 would
-// give, bit for bit.
-template <bool SHORTCUT>
+// law evaluated at v_19.
+//
+// FAST = false is the reference's loop statement by statement.  FAST = true gives the same values
+// bit for bit with less work:
+//  * the law's prefactor 1/(2 V0) exp(...) depends only on the state before the solve, which every
+//    iteration restarts from, so it is evaluated once; the state update (another exp) is needed
+//    only at the last evaluation point, so it is evaluated once after the loop;
+//  * when an iterate repeats (a fixed point v_k = v_(k-1), or a 2-cycle v_k = v_(k-2)) every later
+//    iteration is known and the loop stops with the values iteration 20 would give.
+template <bool FAST>
 __device__ __forceinline__ NewtonOut rsf_newton(int friclaw, double dt, const NewtonSolve &s, double v0) {
+  const RsfParams &p = s.r;
   double vt = v0;
   double stateTmp = s.state0, thTmp = s.th0, taoc_new = 0.0;
-  double vA = 0.0, stA = 0.0, thA = 0.0, tcA = 0.0;  // v_(k-2) and the law evaluated at it
+  double tmpc = 0.0;
+  if (FAST) tmpc = (friclaw == 3) ? 1.0 / (2.0 * p.V0) * exp((p.f0 + p.B * log(p.V0 * s.state0 / p.L)) / p.A)
+                                  : 1.0 / (2.0 * p.V0) * exp(s.state0 / p.A);
+  double v_eval = v0;                        // FAST: where the law was last evaluated
+  double vA = 0.0, thA = 0.0, tcA = 0.0;     // FAST: v_(k-2) and the law evaluated at it
   int iv, executed = 0;
   for (iv = 1; iv <= 20; ++iv) {
     ++executed;
-    stateTmp = s.state0;
     double xmu, dxmudv;
-    rsf_law(friclaw, vt, stateTmp, s.r, dt, xmu, dxmudv);
+    if (FAST) {
+      v_eval = vt;
+      const double tmp = (vt + 1.e-30) * tmpc;
+      xmu = p.A * log(tmp + sqrt(tmp * tmp + 1.0));
+      dxmudv = p.A * tmpc / sqrt(1.0 + tmp * tmp);
+    } else {
+      stateTmp = s.state0;
+      rsf_law(friclaw, vt, stateTmp, p, dt, xmu, dxmudv);
+    }
     double rsfeq, dr;
     if (friclaw < 5) {
       thTmp = s.th0;
-      const double thdot = -vt / s.r.L * (thTmp - fabs(s.tn));
+      const double thdot = -vt / p.L * (thTmp - fabs(s.tn));
       thTmp = thTmp + thdot * dt;
       taoc_new = xmu * thTmp;
       rsfeq = vt + s.Tc * (taoc_new * 0.5 - s.trial);
@@ -84,7 +112,7 @@ __device__ __forceinline__ NewtonOut rsf_newton(int friclaw, double dt, const Ne
     if (fabs(rsfeq / dr) < 1.e-14 * fabs(vt) && fabs(rsfeq) < 1.e-6 * fabs(vt)) break;
     const double vn = vt - rsfeq / dr;
     const double vnew = (vn <= 0.0) ? vt / 2.0 : vn;
-    if (SHORTCUT && iv < 20) {
+    if (FAST && iv < 20) {
       if (vnew == vt) {  // fixed point: v_20 = v_19 = vt
         iv = 21;
         break;
@@ -93,7 +121,7 @@ __device__ __forceinline__ NewtonOut rsf_newton(int friclaw, double dt, const Ne
         if ((20 - iv) % 2 == 0) {
           vt = vnew;  // v_20 = vA, v_19 = vt: the evaluation just made
         } else {      // v_20 = vt, v_19 = vA: the previous evaluation
-          stateTmp = stA;
+          v_eval = vA;
           thTmp = thA;
           taoc_new = tcA;
         }
@@ -101,12 +129,14 @@ __device__ __forceinline__ NewtonOut rsf_newton(int friclaw, double dt, const Ne
         break;
       }
     }
-    vA = vt;
-    stA = stateTmp;
-    thA = thTmp;
-    tcA = taoc_new;
+    if (FAST) {
+      vA = vt;
+      thA = thTmp;
+      tcA = taoc_new;
+    }
     vt = vnew;
   }
+  if (FAST) stateTmp = rsf_state(friclaw, v_eval, s.state0, p, dt);
   NewtonOut o;
   o.v = vt;
   o.state = stateTmp;

@@ -133,8 +133,9 @@ class GpuSolver:
     def enable_mlp(self, on=True):
         self._rc(self.lib.eqd_gpu_mlp_enable(self._h, int(bool(on))), "eqd_gpu_mlp_enable")
 
-    def replay(self, learned=False, shortcut=True, values=False):
-        """Re-solve the logged records: counts (+ converged slip rates when values=True)."""
+    def replay(self, learned=False, fast=True, values=False):
+        """Re-solve the logged records from the plain or learned guess, with the fault kernel's
+        loop (fast) or the reference's loop verbatim: counts (+ slip rates when values=True)."""
         counts = (C.c_int64 * 4)()
         v = None
         vp = None
@@ -143,7 +144,7 @@ class GpuSolver:
             self._rc(self.lib.eqd_gpu_newton_records(self._h, None, 0, C.byref(n)), "eqd_gpu_newton_records")
             v = np.zeros(n.value)
             vp = v.ctypes.data_as(N.c_double_p)
-        self._rc(self.lib.eqd_gpu_newton_replay(self._h, int(bool(learned)), int(bool(shortcut)), counts, vp),
+        self._rc(self.lib.eqd_gpu_newton_replay(self._h, int(bool(learned)), int(bool(fast)), counts, vp),
                  "eqd_gpu_newton_replay")
         out = dict(zip(["iterations", "ivmax_hits", "executed", "records"], list(counts)))
         return (out, v) if values else out

@@ -215,10 +215,12 @@ int eqd_gpu_mlp_get(eqd_context *ctx, float *params, float *norm);
 int eqd_gpu_mlp_set(eqd_context *ctx, const float *params, const float *norm);
 /* on = 1 uses the loaded model as the Newton initial guess, on = 0 the plain one. */
 int eqd_gpu_mlp_enable(eqd_context *ctx, int32_t on);
-/* Re-solves every logged record from the plain (learned = 0) or learned initial guess, with or
- * without the repeated-iterate shortcut: counts = {iterations as the reference counts them,
- * solves that reached 20, iterations executed, records}; v_host[records] may be NULL. */
-int eqd_gpu_newton_replay(eqd_context *ctx, int32_t learned, int32_t shortcut, int64_t counts[4],
+/* Re-solves every logged record from the plain (learned = 0) or learned initial guess, with the
+ * loop the fault kernel runs (fast = 1: loop-invariant law terms evaluated once, early stop on a
+ * repeated iterate, same values bit for bit) or the reference's loop verbatim (fast = 0):
+ * counts = {iterations as the reference counts them, solves that reached 20, iterations
+ * executed, records}; v_host[records] may be NULL. */
+int eqd_gpu_newton_replay(eqd_context *ctx, int32_t learned, int32_t fast, int64_t counts[4],
                           double *v_host);
 /* Loss sum((y - t)^2) / (2 n) and its gradient for a model and a batch, computed by the training
  * kernel: x[n][6] normalised inputs, t[n] normalised targets (gradient checks). */

@@ -1,8 +1,9 @@
 """Learned Newton initial guess and the logged-solve machinery.
 
 * the tensor-core training kernel's loss and gradient against the numpy reference (mlp_ref);
-* logged solves replay bit for bit, with and without the repeated-iterate shortcut, and the
-  shortcut keeps the reference's iteration count while executing fewer iterations;
+* logged solves replay bit for bit, both with the loop the fault kernel runs (loop-invariant law
+  terms evaluated once, early stop on a repeated iterate) and with the reference's loop verbatim,
+  with the reference's iteration count;
 * training on solves logged by the plain method lowers the loss; iteration counts of the plain
   and the learned guess are reported; every solve converges to the same slip rate from either
   guess; the binary32 form with the learned guess stays within the accuracy budget.
@@ -52,14 +53,14 @@ def test_logged_solves_replay_bit_for_bit(c1_logged):
     s, case = c1_logged
     rec = s.newton_records()
     assert rec.shape == (80 * case.npair, 16)
-    full, v_full = s.replay(learned=False, shortcut=False, values=True)
-    short, v_short = s.replay(learned=False, shortcut=True, values=True)
-    print("all iterations", full, "shortcut", short)
-    assert np.array_equal(v_full, rec[:, 14])
-    assert np.array_equal(v_short, rec[:, 14])
-    assert full["iterations"] == short["iterations"] == int(rec[:, 15].sum())
-    assert full["executed"] == full["iterations"]
-    assert short["executed"] < full["executed"]
+    ref, v_ref = s.replay(learned=False, fast=False, values=True)
+    fast, v_fast = s.replay(learned=False, fast=True, values=True)
+    print("reference loop", ref, "fault-kernel loop", fast)
+    assert np.array_equal(v_ref, rec[:, 14])
+    assert np.array_equal(v_fast, rec[:, 14])
+    assert ref["iterations"] == fast["iterations"] == int(rec[:, 15].sum())
+    assert ref["executed"] == ref["iterations"]
+    assert fast["executed"] <= ref["executed"]
 
 
 def test_learned_guess_trains_and_converges_to_the_same_solutions(c1_logged):
