@@ -65,6 +65,9 @@ NODE_BYTES = {"fp64": (152, 536), "fp32": (148, 340)}
 NCU_TRAFFIC_PER_UNIT = {("elem_interior", "records", 1): (105.420032e6 + 10.960384e6) / 1125000,
                         ("elem_pml", "records", 1): (256.453376e6 + 106.076672e6) / 1402000}
 JOB_STEPS = {"C0": 1000, "C1": 4000}
+# the result a host program reads after every step: fric rows 71-76 (slip s/d/n, slip rate s/d,
+# peak slip rate) of every fault pair
+RESULT_ROWS = [71, 72, 73, 74, 75, 76]
 NODE_GATHER_BYTES = {"fp64": 48 + 24, "fp32": 24 + 12}
 PML_NODE_EXTRA = {"fp64": 72, "fp32": 36}
 FP64_FLOPS_PER_ELEM = {"interior": 2 * 423, "pml": 2 * 470}
@@ -269,33 +272,44 @@ def bench_ours(args, world, rank, local):
     host_bytes_in = sum(v.nbytes for k, v in case.arrays.items() if v is not None)
     setup_s = time.perf_counter() - t_setup
     npair = case.npair
-    d2h_per_step = (100 * npair + npair) * 8  # fric + fnft after every step
+    d2h_per_step = len(RESULT_ROWS) * npair * 8  # the step's result rows of fric
+    from eqdyna_gb300.autotune import tuned_options
+    launch = tuned_options(args.config, local) if (args.tuned and args.precision == "fp32") else {}
     args.learned = int(bool(args.learned) and case.scalars.friclaw in (3, 4))  # rate-and-state only
     nlog = min(args.log_steps * args.log_stride, job) if args.learned else 0
 
     # ---- end to end: the whole job through the C ABI with host buffers ----
     e2e_case = case.clone()
-    fr = np.zeros_like(e2e_case.arrays["fric"])
-    fn = np.zeros_like(e2e_case.arrays["fnft"])
+    rows = RESULT_ROWS
+    pinned = N.PinnedArray((len(rows), npair))
     barrier(world)
     t0 = time.perf_counter()
     s = GpuSolver(e2e_case, precision=args.precision, learned_guess=args.learned, device=local,
-                  table_layout=args.tables)
-    done, train_s, hist = 0, 0.0, None
+                  table_layout=args.tables, **launch)
+    t_init = time.perf_counter() - t0
+    init_phases = s.init_times()
+    done, train_s, hist, warm_s = 0, 0.0, None, 0.0
     if args.learned:  # plain warm-up whose Newton solves are the training data, then training
+        t1 = time.perf_counter()
         s.newton_log(nlog // args.log_stride, args.log_stride)
         for _ in range(nlog):
             s.step(1)
-            s.fetch_fault(fr, fn)
+            s.fetch_fric_rows(rows, pinned.array)
         done = nlog
+        warm_s = time.perf_counter() - t1
         t1 = time.perf_counter()
         hist = s.train_mlp(epochs=args.epochs, batch=4096, lr=1e-3, holdout=0.05, seed=20261203)
         train_s = time.perf_counter() - t1
+    t1 = time.perf_counter()
     for _ in range(job - done):
         s.step(1)
-        s.fetch_fault(fr, fn)
+        s.fetch_fric_rows(rows, pinned.array)
+    steps_s = time.perf_counter() - t1
+    t1 = time.perf_counter()
     s.fetch()
+    fetch_s = time.perf_counter() - t1
     e2e_s = time.perf_counter() - t0
+    pinned.close()
     job_newton = s.newton_counts()
     learned = None
     if args.learned:
@@ -308,12 +322,14 @@ def bench_ours(args, world, rank, local):
                    "holdout_loss": round(hist["holdout_loss"], 5),
                    "replay_plain_guess": plain, "replay_learned_guess": guess, "job_newton": job_newton}
     s.close()
+    e2e_breakdown = {"init_s": round(t_init, 2), "init_phases_s": init_phases, "logged_warmup_s": round(warm_s, 2), "train_s": round(train_s, 2),
+                     "steps_s": round(steps_s, 2), "final_fetch_s": round(fetch_s, 2)}
     e2e_s = allreduce_max(e2e_s, world)
     del e2e_case
 
     # ---- device-timed steps (inputs resident in HBM) ----
     s = GpuSolver(case.clone(), precision=args.precision, learned_guess=args.learned, device=local,
-                  table_layout=args.tables)
+                  table_layout=args.tables, **launch)
     if args.learned:
         s.set_mlp(params, norm)
     s.step(args.warmup)
@@ -382,13 +398,16 @@ def bench_ours(args, world, rank, local):
                        "l2": f"inputs larger than L2: working set {working_set / 1e9:.2f} GB per step "
                              "vs 129 MB L2, no flush",
                        "element_tables": {k: (v["layout"], v["records"]) for k, v in tables.items()},
+                       "launch": launch or "defaults",
                        "parallelism": "replicas" if world > 1 else "single GPU",
                        "setup_s": round(setup_s, 1), "wall_ms_per_step": wall * 1e3 / args.steps},
             "e2e": {"value": ne * job * world / e2e_s, "unit": UNIT, "steps": job,
                     "h2d_bytes_per_step": int(host_bytes_in / job),
                     "d2h_bytes_per_step": int(d2h_per_step + host_bytes_in / job),
+                    "breakdown": e2e_breakdown,
                     "note": "whole job through the C ABI: init (every host table to the device), each step "
-                            "followed by a read of the fault state (fric, fnft), final fetch of every array"
+                            "followed by a read of its result (fric rows 71-76 into pinned host memory), "
+                            "final fetch of every array"
                             + ("; the first steps run the plain Newton with solve logging, then training"
                                if args.learned else "")},
             "gpu_launches": int(stats["kernel_launches"]),
@@ -413,6 +432,7 @@ def main():
     ap.add_argument("--log-stride", type=int, default=10, help="one logged step in this many")
     ap.add_argument("--epochs", type=int, default=8)
     ap.add_argument("--job-steps", type=int, default=0, help="steps of the end-to-end job (0: the config's)")
+    ap.add_argument("--tuned", type=int, default=1, help="use the autotuned launch shapes when recorded")
     ap.add_argument("--tables", default="auto", choices=["auto", "streamed", "records"],
                     help="binary32 element-table layout")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])

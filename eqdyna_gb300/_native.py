@@ -68,9 +68,9 @@ INT_ARRAYS = {n for n, t in HOST_ARRAY_FIELDS + FAULT_FIELDS + STATION_FIELDS if
 
 class EqdOptions(C.Structure):
     _fields_ = [("precision", C.c_int32), ("learned_guess", C.c_int32),
-                ("record_tp_hist", C.c_int32), ("block_elem", C.c_int32),
+                ("record_tp_hist", C.c_int32), ("tile_shape", C.c_int32),
                 ("use_graph", C.c_int32), ("device", C.c_int32), ("table_layout", C.c_int32),
-                ("reserved", C.c_int32)]
+                ("block_node", C.c_int32), ("block_fault", C.c_int32), ("reserved", C.c_int32)]
 
 
 PREC_FP64 = 0
@@ -172,6 +172,19 @@ def gpu_lib():
         for name in ("eqd_gpu_newton_log", "eqd_gpu_newton_records", "eqd_gpu_mlp_train", "eqd_gpu_mlp_get",
                      "eqd_gpu_mlp_set", "eqd_gpu_mlp_enable", "eqd_gpu_newton_replay", "eqd_mlp_gradient"):
             getattr(lib, name).restype = C.c_int
+        lib.eqd_gpu_fetch_fric_rows.argtypes = [C.c_void_p, C.POINTER(C.c_int32), C.c_int32, d_p]
+        lib.eqd_gpu_fetch_fric_rows.restype = C.c_int
+        lib.eqd_host_alloc.argtypes = [C.c_int64]
+        lib.eqd_host_alloc.restype = C.c_void_p
+        lib.eqd_host_free.argtypes = [C.c_void_p]
+        lib.eqd_host_free.restype = C.c_int
+        lib.eqd_gpu_init_times.argtypes = [C.c_void_p, d_p]
+        lib.eqd_gpu_init_times.restype = C.c_int
+        lib.eqd_ensemble_create.argtypes = [C.POINTER(C.c_void_p), C.c_int32, C.POINTER(C.c_void_p)]
+        lib.eqd_ensemble_step.argtypes = [C.c_void_p, C.c_int32]
+        lib.eqd_ensemble_destroy.argtypes = [C.c_void_p]
+        for name in ("eqd_ensemble_create", "eqd_ensemble_step", "eqd_ensemble_destroy"):
+            getattr(lib, name).restype = C.c_int
         lib.eqd_gpu_newton_counts.argtypes = [C.c_void_p, C.POINTER(C.c_int64)]
         lib.eqd_gpu_newton_counts.restype = C.c_int
         lib.eqd_gpu_table_info.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_int64)]
@@ -186,8 +199,30 @@ def gpu_lib():
 GPU_SYMBOLS = ["eqd_gpu_init", "eqd_gpu_step", "eqd_gpu_fetch", "eqd_gpu_fetch_fault",
                "eqd_gpu_finalize", "eqd_gpu_status_string", "eqd_gpu_stats", "eqd_gpu_time",
                "eqd_gpu_profile", "eqd_gpu_kernel_time", "eqd_gpu_newton_counts", "eqd_gpu_table_info",
+               "eqd_gpu_fetch_fric_rows", "eqd_host_alloc", "eqd_host_free",
+               "eqd_ensemble_create", "eqd_ensemble_step", "eqd_ensemble_destroy", "eqd_gpu_init_times",
                "eqd_gpu_newton_log", "eqd_gpu_newton_records", "eqd_gpu_mlp_train", "eqd_gpu_mlp_get",
                "eqd_gpu_mlp_set", "eqd_gpu_mlp_enable", "eqd_gpu_newton_replay", "eqd_mlp_gradient",
                "eqd_gpu_fp64_fma_peak"]
 CASE_SYMBOLS = ["eqd_case_build", "eqd_case_view", "eqd_case_array_len", "eqd_case_dims",
                 "eqd_case_lines", "eqd_case_free", "eqd_case_last_error"]
+
+
+class PinnedArray:
+    """A numpy view of page-locked host memory (eqd_host_alloc); freed by close()."""
+
+    def __init__(self, shape, dtype=None):
+        import numpy as np
+        dtype = np.dtype(dtype or np.float64)
+        n = int(np.prod(shape)) * dtype.itemsize
+        lib = gpu_lib()
+        self._p = lib.eqd_host_alloc(max(n, 1))
+        if not self._p:
+            raise EqdError(2, "eqd_host_alloc")
+        buf = (C.c_char * max(n, 1)).from_address(self._p)
+        self.array = np.frombuffer(buf, dtype=dtype, count=int(np.prod(shape))).reshape(shape)
+
+    def close(self):
+        if self._p:
+            gpu_lib().eqd_host_free(self._p)
+            self._p = None

@@ -111,11 +111,10 @@ struct TabCommon {
   static constexpr int STR = MU + 1;
 };
 
-// Gathers the binary32 node data of this CTA's tile; returns the tile's node count.
-__device__ __forceinline__ int stage_nodes(const ElemGroup<float> &g, const float *__restrict__ vel32,
+// Gathers the binary32 node data of tile t; returns the tile's node count.
+__device__ __forceinline__ int stage_nodes(const ElemGroup<float> &g, int t, const float *__restrict__ vel32,
                                            const float *__restrict__ dl32, int nnode, int Mmax, float *sv,
                                            float *sd, int &nb) {
-  const int t = blockIdx.x;
   nb = g.tile_node_ptr[t];
   const int M = g.tile_node_ptr[t + 1] - nb;
   for (int j = threadIdx.x; j < M; j += blockDim.x) {

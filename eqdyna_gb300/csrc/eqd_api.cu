@@ -11,6 +11,7 @@
 #include "mlp_common.cuh"
 
 #include <algorithm>
+#include <chrono>
 #include <tuple>
 #include <unordered_map>
 
@@ -25,6 +26,7 @@ using namespace eqd;
 
 struct eqd_context {
   Context c;
+  double init_ms[8] = {};  // wall time of the setup phases (eqd_gpu_init_times)
   // host-side maps between the Fortran numbering and the device layout
   std::vector<int> node_dev, node_orig;          // original node (0-based) <-> device id
   std::vector<int> gi_orig, gp_orig;             // device element slot -> original element
@@ -286,6 +288,12 @@ int validate(const eqd_scalars *s, const eqd_host_arrays *a) {
 }
 
 int build_device_state(eqd_context &X, const eqd_scalars &s, const eqd_host_arrays &a) {
+  auto t_last = std::chrono::steady_clock::now();
+  auto mark = [&](int k) {
+    const auto t = std::chrono::steady_clock::now();
+    X.init_ms[k] += std::chrono::duration<double, std::milli>(t - t_last).count();
+    t_last = t;
+  };
   Context &c = X.c;
   c.sc = s;
   const int nn = a.nnode, ne = a.nelem;
@@ -399,6 +407,7 @@ int build_device_state(eqd_context &X, const eqd_scalars &s, const eqd_host_arra
   }
   c.f_is_acc = 1;
 
+  mark(0);
   // ---- elements ----
   X.gi_orig.clear();
   X.gp_orig.clear();
@@ -411,9 +420,12 @@ int build_device_state(eqd_context &X, const eqd_scalars &s, const eqd_host_arra
   const bool body = (s.rdampm != 0.0) || (s.C_elastic == 0);
   if (c.fp32) {
     if (s.C_Q == 1) return EQD_ERR_UNSUPPORTED;  // Q memory variables: binary64 form only
-    brick_order(a, X.gi_orig, 4, 4, 8);
-    brick_order(a, X.gp_orig, 4, 4, 8);
+    const int ts = c.opt.tile_shape > 0 ? c.opt.tile_shape : (4 | 8 << 8 | 4 << 16);
+    const int bx = ts & 255, by = (ts >> 8) & 255, bz = (ts >> 16) & 255;
+    brick_order(a, X.gi_orig, bx, bz, by);
+    brick_order(a, X.gp_orig, bx, bz, by);
   }
+  mark(1);
   for (int grp = 0; grp < 2; ++grp) {
     const std::vector<int> &ids = grp == 0 ? X.gi_orig : X.gp_orig;
     ElemGroup<double> &g = grp == 0 ? c.gi64 : c.gp64;
@@ -495,9 +507,11 @@ int build_device_state(eqd_context &X, const eqd_scalars &s, const eqd_host_arra
         qc[4 * (size_t)m + i] = wks * 8.0;
       }
     }
+    mark(2);
     if (c.fp32) {
       ElemGroup<float> &h = grp == 0 ? c.gi32 : c.gp32;
       RC(build_tiles(c, h, conn, grp == 0 ? tile_size_interior() : tile_size_pml()));
+      mark(3);
       h.ld = h.ntiles * h.tile;  // whole tiles: every (component, tile) chunk is one aligned bulk copy
       const size_t um = (size_t)m, ld = (size_t)h.ld;
       // record-indexed layout: one record per distinct binary32 (geometry, material) combination
@@ -593,6 +607,7 @@ int build_device_state(eqd_context &X, const eqd_scalars &s, const eqd_host_arra
       if (grp == 1 && any_s0) RC(dupload(c, h.stress0, to_f32_rows(st0, um, ld)));
       if (!porep.empty()) RC(dupload(c, h.porep, to_f32_rows(porep, um, ld)));
       if (!pstr.empty()) RC(dupload(c, h.pstrain, pstr));
+      mark(4);
       continue;
     }
     RC(dupload(c, g.conn, conn));
@@ -618,6 +633,7 @@ int build_device_state(eqd_context &X, const eqd_scalars &s, const eqd_host_arra
     EQD_CUDA_OK(cudaMemset(c.dl32, 0, 3 * (size_t)nn * sizeof(float)));
   }
 
+  mark(4);
   // ---- fault ----
   const int npair = (a.ntotft >= 1 && a.nftnd) ? a.nftnd[0] : 0;
   c.npair = npair;
@@ -699,6 +715,7 @@ int build_device_state(eqd_context &X, const eqd_scalars &s, const eqd_host_arra
       RC(dupload(c, c.offhist, hh));
     }
   }
+  mark(5);
   // ---- step bookkeeping ----
   RC(dalloc(c, c.d_nt, 1));
   RC(dalloc(c, c.d_err, 1));
@@ -863,6 +880,17 @@ int eqd_gpu_init(const eqd_scalars *s, const eqd_host_arrays *a, const eqd_optio
     return EQD_ERR_CUDA;
   }
   c.fp32 = (c.opt.precision == EQD_PREC_FP32);
+  {  // launch shapes (eqdyna_gb300.autotune chooses them; 0 = default)
+    const int ts = c.opt.tile_shape, bx = ts & 255, by = (ts >> 8) & 255, bz = (ts >> 16) & 255;
+    const int bn = c.opt.block_node, bf = c.opt.block_fault;
+    const bool ok = (ts == 0 || (bx * by * bz == tile_size_interior() && (ts >> 24) == 0)) &&
+                    (bn == 0 || bn == 64 || bn == 128 || bn == 256 || bn == 512) &&
+                    (bf == 0 || bf == 32 || bf == 64 || bf == 128);
+    if (!ok) {
+      delete X;
+      return EQD_ERR_INPUT;
+    }
+  }
   rc = build_device_state(*X, *s, *a);
   if (!rc && c.opt.learned_guess) rc = mlp_init(c);
   if (!rc && cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking) != cudaSuccess) rc = EQD_ERR_CUDA;
@@ -888,7 +916,7 @@ int eqd_gpu_step(eqd_context *X, int32_t nt_begin, int32_t nsteps) {
   }
   int done = 0;
   int64_t launches = 0;
-  const int per_step = 3 + (c.gp64.ne > 0 || c.gp32.ne > 0 ? 1 : 0);
+  const int per_step = 3 + (c.gp64.ne > 0 || c.gp32.ne > 0 ? 1 : 0) + (c.sc.friclaw == 5 && c.tp_hist ? 1 : 0);
   if (c.profile) {
     RC(ensure_events(c, nsteps));
     for (; done < nsteps; ++done) RC(launch_step(c, &c.prof_events[(size_t)kEventsPerStep * done]));
@@ -940,6 +968,36 @@ int eqd_gpu_fetch_fault(eqd_context *X, double *fric, double *fnft) {
       for (int k = 0; k < 100; ++k) fric[100 * (size_t)i + k] = fr[k * (size_t)np + i];
   }
   if (fnft) EQD_CUDA_OK(cudaMemcpy(fnft, c.fnft, np * sizeof(double), cudaMemcpyDeviceToHost));
+  return EQD_OK;
+}
+
+int eqd_gpu_fetch_fric_rows(eqd_context *X, const int32_t *rows, int32_t nrows, double *dst) {
+  if (!X) return EQD_ERR_STATE;
+  if (nrows < 0 || (nrows > 0 && (!rows || !dst))) return EQD_ERR_INPUT;
+  Context &c = X->c;
+  const int np = c.npair;
+  for (int r = 0; r < nrows; ++r)
+    if (rows[r] < 1 || rows[r] > 100) return EQD_ERR_INPUT;
+  if (np == 0 || nrows == 0) return EQD_OK;
+  cudaSetDevice(c.device);
+  for (int r = 0; r < nrows; ++r)
+    EQD_CUDA_OK(cudaMemcpyAsync(dst + (size_t)r * np, c.fric + (size_t)(rows[r] - 1) * np, np * sizeof(double),
+                                cudaMemcpyDeviceToHost, c.stream));
+  EQD_CUDA_OK(cudaStreamSynchronize(c.stream));
+  return EQD_OK;
+}
+
+void *eqd_host_alloc(int64_t bytes) {
+  void *p = nullptr;
+  if (bytes <= 0 || cudaHostAlloc(&p, (size_t)bytes, cudaHostAllocDefault) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return p;
+}
+
+int eqd_host_free(void *p) {
+  if (p && cudaFreeHost(p) != cudaSuccess) return EQD_ERR_CUDA;
   return EQD_OK;
 }
 
@@ -1195,6 +1253,126 @@ int eqd_gpu_newton_replay(eqd_context *X, int32_t learned, int32_t fast, int64_t
   return EQD_OK;
 }
 
+// ---- ensembles ---------------------------------------------------------------------------------
+struct eqd_ensemble {
+  std::vector<eqd_context *> members;
+  std::vector<Context *> ctx;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  void *nf = nullptr;  // node / fault argument tables
+  void *eb = nullptr;  // element argument tables
+  cudaGraphExec_t graph = nullptr;
+};
+
+namespace {
+int ensemble_refresh(eqd_ensemble &E) {
+  EQD_CUDA_OK(cudaStreamSynchronize(E.stream));  // no launch reads the tables while they change
+  RC(node_fault_batch_update(&E.nf, E.ctx.data(), (int)E.ctx.size()));
+  std::vector<ElemConst> k(E.ctx.size());
+  for (size_t i = 0; i < E.ctx.size(); ++i) k[i] = make_elem_const(*E.ctx[i]);
+  return elem_batch_update(&E.eb, E.ctx.data(), (int)E.ctx.size(), k.data());
+}
+
+int ensemble_launch_step(eqd_ensemble &E) {
+  RC(launch_node_update_batched(E.nf, E.stream));
+  RC(launch_elements_batched(E.eb, E.stream, 2));
+  return launch_fault_batched(E.nf, E.stream);
+}
+}  // namespace
+
+int eqd_ensemble_create(eqd_context *const *members, int32_t n, eqd_ensemble **out) {
+  if (!members || n <= 0 || !out) return EQD_ERR_INPUT;
+  auto *E = new eqd_ensemble();
+  for (int i = 0; i < n; ++i) {
+    if (!members[i] || members[i]->c.device != members[0]->c.device) {
+      delete E;
+      return EQD_ERR_INPUT;
+    }
+    E->members.push_back(members[i]);
+    E->ctx.push_back(&members[i]->c);
+  }
+  E->device = members[0]->c.device;
+  cudaSetDevice(E->device);
+  int rc = EQD_OK;
+  if (cudaStreamCreateWithFlags(&E->stream, cudaStreamNonBlocking) != cudaSuccess) rc = EQD_ERR_CUDA;
+  if (!rc) {
+    for (auto *X : E->members) cudaStreamSynchronize(X->c.stream);
+    rc = ensemble_refresh(*E);
+  }
+  if (rc) {
+    eqd_ensemble_destroy(E);
+    return rc;
+  }
+  *out = E;
+  return EQD_OK;
+}
+
+int eqd_ensemble_step(eqd_ensemble *E, int32_t nsteps) {
+  if (!E) return EQD_ERR_STATE;
+  if (nsteps < 0) return EQD_ERR_INPUT;
+  if (nsteps == 0) return EQD_OK;
+  cudaSetDevice(E->device);
+  for (auto *X : E->members) RC(ensure_times(*X, X->c.nt + nsteps));
+  RC(ensemble_refresh(*E));
+  int done = 0;
+  bool first = false;
+  for (auto *c : E->ctx) first |= c->f_is_acc != 0;
+  if (first) {  // members fresh from init consume their stored acceleration in this step
+    RC(ensemble_launch_step(*E));
+    for (auto *c : E->ctx) c->f_is_acc = 0;
+    RC(ensemble_refresh(*E));
+    ++done;
+  }
+  if (nsteps - done >= kGraphSteps) {
+    if (!E->graph) {
+      cudaGraph_t g;
+      EQD_CUDA_OK(cudaStreamBeginCapture(E->stream, cudaStreamCaptureModeThreadLocal));
+      int rc = EQD_OK;
+      for (int k = 0; k < kGraphSteps && !rc; ++k) rc = ensemble_launch_step(*E);
+      const cudaError_t e = cudaStreamEndCapture(E->stream, &g);
+      if (rc) return rc;
+      EQD_CUDA_OK(e);
+      const cudaError_t ei = cudaGraphInstantiate(&E->graph, g, 0);
+      cudaGraphDestroy(g);
+      if (ei != cudaSuccess) {
+        E->graph = nullptr;
+        return EQD_ERR_CUDA;
+      }
+    }
+    while (nsteps - done >= kGraphSteps) {
+      EQD_CUDA_OK(cudaGraphLaunch(E->graph, E->stream));
+      done += kGraphSteps;
+    }
+  }
+  for (; done < nsteps; ++done) RC(ensemble_launch_step(*E));
+  EQD_CUDA_OK(cudaStreamSynchronize(E->stream));
+  EQD_CUDA_OK(cudaGetLastError());
+  int status = EQD_OK;
+  for (auto *X : E->members) {
+    Context &c = X->c;
+    int err = 0;
+    EQD_CUDA_OK(cudaMemcpy(&err, c.d_err, sizeof(int), cudaMemcpyDeviceToHost));
+    c.nt += nsteps;
+    c.time = X->times[c.nt];
+    c.elem_updates += (int64_t)c.nelem * nsteps;
+    if (err & 2) status = EQD_ERR_TIMEOUT;
+    else if (err && !status) status = EQD_ERR_NAN;
+  }
+  return status;
+}
+
+int eqd_ensemble_destroy(eqd_ensemble *E) {
+  if (!E) return EQD_OK;
+  cudaSetDevice(E->device);
+  if (E->stream) cudaStreamSynchronize(E->stream);
+  if (E->graph) cudaGraphExecDestroy(E->graph);
+  node_fault_batch_free(E->nf);
+  elem_batch_free(E->eb);
+  if (E->stream) cudaStreamDestroy(E->stream);
+  delete E;
+  return EQD_OK;
+}
+
 int eqd_gpu_newton_counts(eqd_context *X, int64_t out[4]) {
   if (!X) return EQD_ERR_STATE;
   if (!out) return EQD_ERR_INPUT;
@@ -1204,6 +1382,13 @@ int eqd_gpu_newton_counts(eqd_context *X, int64_t out[4]) {
   EQD_CUDA_OK(cudaStreamSynchronize(c.stream));
   EQD_CUDA_OK(cudaMemcpy(st, c.d_stats, sizeof(st), cudaMemcpyDeviceToHost));
   for (int k = 0; k < 4; ++k) out[k] = (int64_t)st[k];
+  return EQD_OK;
+}
+
+int eqd_gpu_init_times(eqd_context *X, double ms[8]) {
+  if (!X) return EQD_ERR_STATE;
+  if (!ms) return EQD_ERR_INPUT;
+  for (int k = 0; k < 8; ++k) ms[k] = X->init_ms[k];
   return EQD_OK;
 }
 

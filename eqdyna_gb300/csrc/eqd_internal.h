@@ -150,6 +150,18 @@ struct Context {
 int launch_node_update(Context &c, cudaStream_t s);
 int launch_elements(Context &c, cudaStream_t s, int part = 2);  // 0 interior, 1 PML, 2 both
 int launch_fault(Context &c, cudaStream_t s);
+
+// Ensembles: one launch per kernel over several contexts.  *_update builds the device argument
+// tables on the first call (handle == null) and refreshes them afterwards (per-member state such
+// as the first-step flag, the time table, the learned guess); the launches read the tables.
+struct ElemConst;
+int node_fault_batch_update(void **handle, Context *const *members, int n);
+int launch_node_update_batched(const void *handle, cudaStream_t s);
+int launch_fault_batched(const void *handle, cudaStream_t s);
+void node_fault_batch_free(void *handle);
+int elem_batch_update(void **handle, Context *const *members, int n, const ElemConst *k);
+int launch_elements_batched(const void *handle, cudaStream_t s, int part);
+void elem_batch_free(void *handle);
 int mlp_init(Context &c);
 void mlp_free(Context &c);
 int newton_log_start(Context &c, int nsteps, int stride);

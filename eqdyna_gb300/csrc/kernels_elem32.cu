@@ -100,7 +100,7 @@ __global__ void __launch_bounds__(kTile)
   }
   __syncthreads();  // barrier initialised before anyone polls it
   int nb;
-  const int M = stage_nodes(g, vel32, dl32, nnode, Mmax, sv, sd, nb);
+  const int M = stage_nodes(g, blockIdx.x, vel32, dl32, nnode, Mmax, sv, sd, nb);
   const bool ok = mbar_wait_bounded(&bar, err);
   const unsigned short *incp = g.tile_incp + g.tile_incp_off[blockIdx.x];
   if (ok) build_slots(incp, M, sinc, slot_of);
@@ -143,7 +143,7 @@ __global__ void __launch_bounds__(kTile)
   }
   __syncthreads();
   int nb;
-  const int M = stage_nodes(g, vel32, dl32, nnode, Mmax, sv, sd, nb);
+  const int M = stage_nodes(g, blockIdx.x, vel32, dl32, nnode, Mmax, sv, sd, nb);
   const bool ok = mbar_wait_bounded(&bar, err);
   const unsigned short *incp = g.tile_incp + g.tile_incp_off[blockIdx.x];
   if (ok) build_slots(incp, M, sinc, slot_of);

@@ -17,6 +17,9 @@
 // (stress, record index, PML axis indices, initial stress, pore pressure) and the incidence list
 // into shared memory while all threads gather the tile's node data; then the element math and the
 // node gather of elem32_common.cuh.
+#include <algorithm>
+#include <vector>
+
 #include "elem32_common.cuh"
 
 namespace eqd {
@@ -93,14 +96,24 @@ __device__ __forceinline__ unsigned row_u32(const float *tab, int row, int col) 
   return reinterpret_cast<const unsigned *>(tab)[row * kTile + col];
 }
 
+// Everything one record-layout element launch reads: the group, the node arrays, the constants
+// and (UNI) the group's single record.
+struct ElemArgs32 {
+  ElemGroup<float> g;
+  const float *vel32, *dl32;
+  float *F, *F9;
+  int nnode, n_int, npml;
+  int *err;
+  ElemConst32 k;
+  RecordParam rp;
+};
+
 template <bool BODY, bool PLASTIC, int HG, bool UNI>
-__global__ void __launch_bounds__(kTile)
-    elem_interior_rec(ElemGroup<float> g, const float *__restrict__ vel32, const float *__restrict__ dl32,
-                      float *__restrict__ F, int nnode, ElemConst32 k, int *__restrict__ err,
-                      const __grid_constant__ RecordParam rp) {
+__device__ __forceinline__ void interior_rec_body(const ElemArgs32 &a, int tile) {
   using L = RecInterior<BODY, PLASTIC, HG>;
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) unsigned long long bar;
+  const ElemGroup<float> &g = a.g;
   const int Mmax = g.max_tile_nodes;
   float *tab = reinterpret_cast<float *>(smem);
   unsigned short *sinc = reinterpret_cast<unsigned short *>(tab + L::NS * kTile);
@@ -108,21 +121,21 @@ __global__ void __launch_bounds__(kTile)
   float *sv = reinterpret_cast<float *>(slot_of + 8 * kTile);
   float *sd = sv + 3 * Mmax;
   const int tid = threadIdx.x;
-  const int e0 = blockIdx.x * kTile;
+  const int e0 = tile * kTile;
   const int ld = g.ld;
   if (tid == 0) {
     mbar_init(&bar, 1);
     mbar_expect_tx(&bar, (unsigned)(L::N * kTile * 4 + 8 * kTile * 2));
-    bulk_g2s(sinc, g.tile_inc + (size_t)blockIdx.x * kTile * 8, 8 * kTile * 2, &bar);
+    bulk_g2s(sinc, g.tile_inc + (size_t)tile * kTile * 8, 8 * kTile * 2, &bar);
     copy_rows(tab, L::STR, g.stress, 6, ld, e0, &bar);
     if (PLASTIC) copy_rows(tab, L::POR, g.porep, 1, ld, e0, &bar);
     copy_rows(tab, L::RID, g.rec_id, 1, ld, e0, &bar);
   }
   __syncthreads();
   int nb;
-  const int M = stage_nodes(g, vel32, dl32, nnode, Mmax, sv, sd, nb);
-  const bool ok = mbar_wait_bounded(&bar, err);
-  const unsigned short *incp = g.tile_incp + g.tile_incp_off[blockIdx.x];
+  const int M = stage_nodes(g, tile, a.vel32, a.dl32, a.nnode, Mmax, sv, sd, nb);
+  const bool ok = mbar_wait_bounded(&bar, a.err);
+  const unsigned short *incp = g.tile_incp + g.tile_incp_off[tile];
   if (ok) build_slots(incp, M, sinc, slot_of);
   if (__syncthreads_or(!ok)) return;
   const int e = e0 + tid;
@@ -130,27 +143,25 @@ __global__ void __launch_bounds__(kTile)
   if (e < g.ne) {
     double *ps = PLASTIC ? g.pstrain + e : nullptr;
     if (UNI) {
-      const UniSrc<L> S{rp, tab, tid, nullptr, 0, 0u, 0u};
-      interior_element<BODY, PLASTIC, HG>(S, sv, sd, Mmax, slot_of, tid, k, ps, g.stress + e, (size_t)ld, fs);
+      const UniSrc<L> S{a.rp, tab, tid, nullptr, 0, 0u, 0u};
+      interior_element<BODY, PLASTIC, HG>(S, sv, sd, Mmax, slot_of, tid, a.k, ps, g.stress + e, (size_t)ld, fs);
     } else {
       const RecSrc<L> S{g.rec + (size_t)row_u32(tab, L::RID, tid) * g.rec_len, tab, tid, nullptr, 0, 0u, 0u};
-      interior_element<BODY, PLASTIC, HG>(S, sv, sd, Mmax, slot_of, tid, k, ps, g.stress + e, (size_t)ld, fs);
+      interior_element<BODY, PLASTIC, HG>(S, sv, sd, Mmax, slot_of, tid, a.k, ps, g.stress + e, (size_t)ld, fs);
     }
   }
   __syncthreads();
-  interior_gather(g, M, nb, incp, sinc, fs, F, nnode);
+  interior_gather(g, M, nb, incp, sinc, fs, a.F, a.nnode);
 }
 
 template <bool BODY, bool S0, int HG, bool UNI>
-__global__ void __launch_bounds__(kTile)
-    elem_pml_rec(ElemGroup<float> g, const float *__restrict__ vel32, const float *__restrict__ dl32,
-                 float *__restrict__ F, float *__restrict__ F9, int nnode, int n_int, int npml,
-                 ElemConst32 k, int *__restrict__ err, const __grid_constant__ RecordParam rp) {
+__device__ __forceinline__ void pml_rec_body(const ElemArgs32 &a, int tile) {
   using L = RecPml<BODY, S0, HG>;
   using C = TabCommon<HG>;
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) unsigned long long bar;
   __shared__ float cw[24];  // UNI: det * shape gradient (3 a + k) of the group's record
+  const ElemGroup<float> &g = a.g;
   const int Mmax = g.max_tile_nodes;
   float *tab = reinterpret_cast<float *>(smem);
   unsigned short *sinc = reinterpret_cast<unsigned short *>(tab + L::NS * kTile);
@@ -158,23 +169,23 @@ __global__ void __launch_bounds__(kTile)
   float *sv = reinterpret_cast<float *>(slot_of + 8 * kTile);
   float *sd = sv + 3 * Mmax;
   const int tid = threadIdx.x;
-  const int e0 = blockIdx.x * kTile;
+  const int e0 = tile * kTile;
   const int ld = g.ld;
   if (tid == 0) {
     mbar_init(&bar, 1);
     mbar_expect_tx(&bar, (unsigned)(L::N * kTile * 4 + 8 * kTile * 2));
-    bulk_g2s(sinc, g.tile_inc + (size_t)blockIdx.x * kTile * 8, 8 * kTile * 2, &bar);
+    bulk_g2s(sinc, g.tile_inc + (size_t)tile * kTile * 8, 8 * kTile * 2, &bar);
     copy_rows(tab, L::STR, g.stress, 15, ld, e0, &bar);
     if (S0) copy_rows(tab, L::ST0, g.stress0, 6, ld, e0, &bar);
     copy_rows(tab, L::RID, g.rec_id, 1, ld, e0, &bar);
     copy_rows(tab, L::ABID, g.ab_id, 2, ld, e0, &bar);
   }
-  if (UNI && tid < 24) cw[tid] = rp.v[C::DET] * rp.v[C::SHP + tid];
+  if (UNI && tid < 24) cw[tid] = a.rp.v[C::DET] * a.rp.v[C::SHP + tid];
   __syncthreads();
   int nb;
-  const int M = stage_nodes(g, vel32, dl32, nnode, Mmax, sv, sd, nb);
-  const bool ok = mbar_wait_bounded(&bar, err);
-  const unsigned short *incp = g.tile_incp + g.tile_incp_off[blockIdx.x];
+  const int M = stage_nodes(g, tile, a.vel32, a.dl32, a.nnode, Mmax, sv, sd, nb);
+  const bool ok = mbar_wait_bounded(&bar, a.err);
+  const unsigned short *incp = g.tile_incp + g.tile_incp_off[tile];
   if (ok) build_slots(incp, M, sinc, slot_of);
   if (__syncthreads_or(!ok)) return;
   const int e = e0 + tid;
@@ -185,28 +196,76 @@ __global__ void __launch_bounds__(kTile)
   if (e < g.ne) {
     const unsigned ab01 = row_u32(tab, L::ABID, tid), ab2 = row_u32(tab, L::ABID + 1, tid);
     if (UNI) {
-      const UniSrc<L> S{rp, tab, tid, g.ab_tab, g.ab_stride, ab01, ab2};
-      pml_element<BODY, S0, HG>(S, sv, sd, Mmax, slot_of, tid, k, g.stress + e, (size_t)ld, es, cfh);
+      const UniSrc<L> S{a.rp, tab, tid, g.ab_tab, g.ab_stride, ab01, ab2};
+      pml_element<BODY, S0, HG>(S, sv, sd, Mmax, slot_of, tid, a.k, g.stress + e, (size_t)ld, es, cfh);
     } else {
       const RecSrc<L> S{rec + (size_t)row_u32(tab, L::RID, tid) * rlen, tab, tid, g.ab_tab, g.ab_stride,
                         ab01, ab2};
-      pml_element<BODY, S0, HG>(S, sv, sd, Mmax, slot_of, tid, k, g.stress + e, (size_t)ld, es, cfh);
+      pml_element<BODY, S0, HG>(S, sv, sd, Mmax, slot_of, tid, a.k, g.stress + e, (size_t)ld, es, cfh);
     }
   }
   __syncthreads();
   if (UNI) {
-    auto w_of = [&](int, int a, float &wx, float &wy, float &wz) {
-      wx = cw[3 * a];
-      wy = cw[3 * a + 1];
-      wz = cw[3 * a + 2];
+    auto w_of = [&](int, int c, float &wx, float &wy, float &wz) {
+      wx = cw[3 * c];
+      wy = cw[3 * c + 1];
+      wz = cw[3 * c + 2];
     };
-    pml_gather(g, M, nb, incp, sinc, es, cfh, w_of, F, F9, nnode, n_int, npml);
+    pml_gather(g, M, nb, incp, sinc, es, cfh, w_of, a.F, a.F9, a.nnode, a.n_int, a.npml);
   } else {
     auto src_of = [&](int el) {
       return RecSrc<L>{rec + (size_t)row_u32(tab, L::RID, el) * rlen, tab, el, nullptr, 0, 0u, 0u};
     };
-    pml_gather(g, M, nb, incp, sinc, es, cfh, w_from_src<HG>(src_of), F, F9, nnode, n_int, npml);
+    pml_gather(g, M, nb, incp, sinc, es, cfh, w_from_src<HG>(src_of), a.F, a.F9, a.nnode, a.n_int, a.npml);
   }
+}
+
+// One group of one context: arguments in parameter space (record values become constant-bank
+// operands in the UNI variant).
+template <bool BODY, bool PLASTIC, int HG, bool UNI>
+__global__ void __launch_bounds__(kTile) elem_interior_rec(const __grid_constant__ ElemArgs32 a) {
+  interior_rec_body<BODY, PLASTIC, HG, UNI>(a, blockIdx.x);
+}
+template <bool BODY, bool S0, int HG, bool UNI>
+__global__ void __launch_bounds__(kTile) elem_pml_rec(const __grid_constant__ ElemArgs32 a) {
+  pml_rec_body<BODY, S0, HG, UNI>(a, blockIdx.x);
+}
+
+// The same group of every member of an ensemble in one launch: each CTA finds its member from the
+// tile prefix sums and copies the member's arguments into shared memory.
+__device__ __forceinline__ int elem_batch_member(const int *__restrict__ start, int n, int b) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (start[mid] <= b) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+__device__ __forceinline__ int load_member(const ElemArgs32 *__restrict__ args, const int *__restrict__ start,
+                                           int n, ElemArgs32 &a) {
+  const int m = elem_batch_member(start, n, blockIdx.x);
+  const int *src = reinterpret_cast<const int *>(args + m);
+  int *dst = reinterpret_cast<int *>(&a);
+  for (int q = threadIdx.x; q < (int)(sizeof(ElemArgs32) / 4); q += blockDim.x) dst[q] = src[q];
+  __syncthreads();
+  return blockIdx.x - start[m];
+}
+template <bool BODY, bool PLASTIC, int HG>
+__global__ void __launch_bounds__(kTile) elem_interior_rec_batched(const ElemArgs32 *__restrict__ args,
+                                                                   const int *__restrict__ start, int n) {
+  __shared__ __align__(16) ElemArgs32 a;
+  const int tile = load_member(args, start, n, a);
+  if (a.g.nrec == 1) interior_rec_body<BODY, PLASTIC, HG, true>(a, tile);
+  else interior_rec_body<BODY, PLASTIC, HG, false>(a, tile);
+}
+template <bool BODY, bool S0, int HG>
+__global__ void __launch_bounds__(kTile) elem_pml_rec_batched(const ElemArgs32 *__restrict__ args,
+                                                              const int *__restrict__ start, int n) {
+  __shared__ __align__(16) ElemArgs32 a;
+  const int tile = load_member(args, start, n, a);
+  if (a.g.nrec == 1) pml_rec_body<BODY, S0, HG, true>(a, tile);
+  else pml_rec_body<BODY, S0, HG, false>(a, tile);
 }
 
 template <class L>
@@ -214,48 +273,117 @@ size_t rec_smem(int Mmax) {
   return (size_t)L::NS * kTile * 4 + 2 * (8 * kTile * 2) + 6 * (size_t)Mmax * 4;
 }
 
-template <bool BODY, bool PLASTIC, int HG, bool UNI>
-int launch_interior_v(Context &c, cudaStream_t s, const ElemConst32 &k) {
-  const ElemGroup<float> &g = c.gi32;
-  const size_t sm = rec_smem<RecInterior<BODY, PLASTIC, HG>>(g.max_tile_nodes);
-  auto kern = elem_interior_rec<BODY, PLASTIC, HG, UNI>;
-  if (allow_smem(kern, sm)) return EQD_ERR_CUDA;
-  kern<<<g.ntiles, kTile, sm, s>>>(g, c.vel32, c.dl32, c.F32, c.nnode, k, c.d_err, c.rec0[0]);
-  return EQD_OK;
-}
-template <bool BODY, bool PLASTIC, int HG>
-int launch_interior(Context &c, cudaStream_t s, const ElemConst32 &k) {
-  return c.gi32.nrec == 1 ? launch_interior_v<BODY, PLASTIC, HG, true>(c, s, k)
-                          : launch_interior_v<BODY, PLASTIC, HG, false>(c, s, k);
+ElemArgs32 elem_args(const Context &c, bool interior, const ElemConst32 &k) {
+  ElemArgs32 a;
+  a.g = interior ? c.gi32 : c.gp32;
+  a.vel32 = c.vel32;
+  a.dl32 = c.dl32;
+  a.F = c.F32;
+  a.F9 = c.F9_32;
+  a.nnode = c.nnode;
+  a.n_int = c.n_int;
+  a.npml = c.npml;
+  a.err = c.d_err;
+  a.k = k;
+  a.rp = c.rec0[interior ? 0 : 1];
+  return a;
 }
 
-template <bool BODY, bool S0, int HG, bool UNI>
-int launch_pml_v(Context &c, cudaStream_t s, const ElemConst32 &k) {
-  const ElemGroup<float> &g = c.gp32;
-  const size_t sm = rec_smem<RecPml<BODY, S0, HG>>(g.max_tile_nodes);
-  auto kern = elem_pml_rec<BODY, S0, HG, UNI>;
-  if (allow_smem(kern, sm)) return EQD_ERR_CUDA;
-  kern<<<g.ntiles, kTile, sm, s>>>(g, c.vel32, c.dl32, c.F32, c.F9_32, c.nnode, c.n_int, c.npml, k, c.d_err,
-                                   c.rec0[1]);
+// Kernel variant of a context's group: template flags (BODY, PLASTIC / S0, HG) as a small code.
+struct Variant {
+  bool body, plastic, s0;
+  int hg;
+};
+Variant variant_of(const Context &c) {
+  return Variant{(c.sc.rdampm != 0.0) || (c.sc.C_elastic == 0), c.sc.C_elastic == 0, c.gp32.stress0 != nullptr,
+                 c.sc.C_hg == 2 ? 2 : 1};
+}
+
+template <bool BODY, bool PLASTIC, int HG>
+int launch_interior(Context &c, cudaStream_t s, const ElemConst32 &k) {
+  const ElemArgs32 a = elem_args(c, true, k);
+  const size_t sm = rec_smem<RecInterior<BODY, PLASTIC, HG>>(a.g.max_tile_nodes);
+  if (a.g.nrec == 1) {
+    auto kern = elem_interior_rec<BODY, PLASTIC, HG, true>;
+    if (allow_smem(kern, sm)) return EQD_ERR_CUDA;
+    kern<<<a.g.ntiles, kTile, sm, s>>>(a);
+  } else {
+    auto kern = elem_interior_rec<BODY, PLASTIC, HG, false>;
+    if (allow_smem(kern, sm)) return EQD_ERR_CUDA;
+    kern<<<a.g.ntiles, kTile, sm, s>>>(a);
+  }
   return EQD_OK;
 }
+
 template <bool BODY, bool S0, int HG>
 int launch_pml(Context &c, cudaStream_t s, const ElemConst32 &k) {
-  return c.gp32.nrec == 1 ? launch_pml_v<BODY, S0, HG, true>(c, s, k) : launch_pml_v<BODY, S0, HG, false>(c, s, k);
+  const ElemArgs32 a = elem_args(c, false, k);
+  const size_t sm = rec_smem<RecPml<BODY, S0, HG>>(a.g.max_tile_nodes);
+  if (a.g.nrec == 1) {
+    auto kern = elem_pml_rec<BODY, S0, HG, true>;
+    if (allow_smem(kern, sm)) return EQD_ERR_CUDA;
+    kern<<<a.g.ntiles, kTile, sm, s>>>(a);
+  } else {
+    auto kern = elem_pml_rec<BODY, S0, HG, false>;
+    if (allow_smem(kern, sm)) return EQD_ERR_CUDA;
+    kern<<<a.g.ntiles, kTile, sm, s>>>(a);
+  }
+  return EQD_OK;
 }
 
 template <int HG>
 int launch_hg(Context &c, cudaStream_t s, const ElemConst32 &k, bool interior) {
-  const bool body = (c.sc.rdampm != 0.0) || (c.sc.C_elastic == 0);
-  const bool plastic = (c.sc.C_elastic == 0);
+  const Variant v = variant_of(c);
   if (interior) {
-    if (plastic) return body ? launch_interior<true, true, HG>(c, s, k) : launch_interior<false, true, HG>(c, s, k);
-    return body ? launch_interior<true, false, HG>(c, s, k) : launch_interior<false, false, HG>(c, s, k);
+    if (v.plastic) return v.body ? launch_interior<true, true, HG>(c, s, k) : launch_interior<false, true, HG>(c, s, k);
+    return v.body ? launch_interior<true, false, HG>(c, s, k) : launch_interior<false, false, HG>(c, s, k);
   }
-  const bool s0 = c.gp32.stress0 != nullptr;
-  if (body) return s0 ? launch_pml<true, true, HG>(c, s, k) : launch_pml<true, false, HG>(c, s, k);
-  return s0 ? launch_pml<false, true, HG>(c, s, k) : launch_pml<false, false, HG>(c, s, k);
+  if (v.body) return v.s0 ? launch_pml<true, true, HG>(c, s, k) : launch_pml<true, false, HG>(c, s, k);
+  return v.s0 ? launch_pml<false, true, HG>(c, s, k) : launch_pml<false, false, HG>(c, s, k);
 }
+
+// ---- ensembles ----------------------------------------------------------------------------------
+template <bool BODY, bool PLASTIC, int HG>
+int launch_interior_batched(const ElemArgs32 *args, const int *start, int n, int tiles, int Mmax, cudaStream_t s) {
+  const size_t sm = rec_smem<RecInterior<BODY, PLASTIC, HG>>(Mmax);
+  auto kern = elem_interior_rec_batched<BODY, PLASTIC, HG>;
+  if (allow_smem(kern, sm)) return EQD_ERR_CUDA;
+  kern<<<tiles, kTile, sm, s>>>(args, start, n);
+  return EQD_OK;
+}
+template <bool BODY, bool S0, int HG>
+int launch_pml_batched(const ElemArgs32 *args, const int *start, int n, int tiles, int Mmax, cudaStream_t s) {
+  const size_t sm = rec_smem<RecPml<BODY, S0, HG>>(Mmax);
+  auto kern = elem_pml_rec_batched<BODY, S0, HG>;
+  if (allow_smem(kern, sm)) return EQD_ERR_CUDA;
+  kern<<<tiles, kTile, sm, s>>>(args, start, n);
+  return EQD_OK;
+}
+template <int HG>
+int launch_batched_hg(const Variant &v, bool interior, const ElemArgs32 *args, const int *start, int n, int tiles,
+                      int Mmax, cudaStream_t s) {
+  if (interior) {
+    if (v.plastic)
+      return v.body ? launch_interior_batched<true, true, HG>(args, start, n, tiles, Mmax, s)
+                    : launch_interior_batched<false, true, HG>(args, start, n, tiles, Mmax, s);
+    return v.body ? launch_interior_batched<true, false, HG>(args, start, n, tiles, Mmax, s)
+                  : launch_interior_batched<false, false, HG>(args, start, n, tiles, Mmax, s);
+  }
+  if (v.body)
+    return v.s0 ? launch_pml_batched<true, true, HG>(args, start, n, tiles, Mmax, s)
+                : launch_pml_batched<true, false, HG>(args, start, n, tiles, Mmax, s);
+  return v.s0 ? launch_pml_batched<false, true, HG>(args, start, n, tiles, Mmax, s)
+              : launch_pml_batched<false, false, HG>(args, start, n, tiles, Mmax, s);
+}
+
+struct ElemBatch {
+  int n = 0;
+  Variant v{};
+  ElemArgs32 *d_args[2] = {nullptr, nullptr};  // interior, PML
+  int *d_start[2] = {nullptr, nullptr};         // [n + 1] tile prefix sums
+  int tiles[2] = {0, 0}, Mmax[2] = {0, 0};
+  std::vector<ElemArgs32> h_args[2];
+};
 
 }  // namespace
 
@@ -267,6 +395,80 @@ int record_length(int hg, bool body) {
 
 int launch_elements_rec(Context &c, cudaStream_t s, const ElemConst32 &k, bool interior) {
   return c.sc.C_hg == 2 ? launch_hg<2>(c, s, k, interior) : launch_hg<1>(c, s, k, interior);
+}
+
+// Builds (or refreshes) the element tables of an ensemble.  Every member must run the binary32
+// form with record-indexed tables and the same kernel variant.
+int elem_batch_update(void **handle, Context *const *m, int n, const ElemConst *kd) {
+  if (n <= 0) return EQD_ERR_INPUT;
+  ElemBatch *b = static_cast<ElemBatch *>(*handle);
+  const Variant v = variant_of(*m[0]);
+  for (int i = 0; i < n; ++i) {
+    const Variant w = variant_of(*m[i]);
+    if (!m[i]->fp32 || w.body != v.body || w.plastic != v.plastic || w.s0 != v.s0 || w.hg != v.hg)
+      return EQD_ERR_UNSUPPORTED;
+    for (int grp = 0; grp < 2; ++grp) {
+      const ElemGroup<float> &g = grp == 0 ? m[i]->gi32 : m[i]->gp32;
+      if (g.ne > 0 && g.nrec == 0) return EQD_ERR_UNSUPPORTED;  // streamed tables
+    }
+  }
+  if (!b) {
+    b = new ElemBatch();
+    b->n = n;
+    b->v = v;
+    for (int grp = 0; grp < 2; ++grp) {
+      std::vector<int> start(n + 1, 0);
+      for (int i = 0; i < n; ++i) {
+        const ElemGroup<float> &g = grp == 0 ? m[i]->gi32 : m[i]->gp32;
+        start[i + 1] = start[i] + (g.ne > 0 ? g.ntiles : 0);
+        b->Mmax[grp] = std::max(b->Mmax[grp], g.max_tile_nodes);
+      }
+      b->tiles[grp] = start[n];
+      if (cudaMalloc(&b->d_start[grp], sizeof(int) * (n + 1)) != cudaSuccess ||
+          cudaMalloc(&b->d_args[grp], sizeof(ElemArgs32) * n) != cudaSuccess) {
+        elem_batch_free(b);
+        return EQD_ERR_OOM;
+      }
+      cudaMemcpy(b->d_start[grp], start.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice);
+      b->h_args[grp].resize(n);
+    }
+    *handle = b;
+  }
+  if (b->n != n) return EQD_ERR_INPUT;
+  for (int grp = 0; grp < 2; ++grp) {
+    for (int i = 0; i < n; ++i) {
+      const ElemConst &q = kd[i];
+      const ElemConst32 k{(float)q.dt, (float)q.rdampk, (float)q.rdampm, (float)q.gz,
+                          (float)q.ccosphi, (float)q.sinphi, (float)q.relax};
+      b->h_args[grp][i] = elem_args(*m[i], grp == 0, k);
+    }
+    EQD_CUDA_OK(cudaMemcpy(b->d_args[grp], b->h_args[grp].data(), sizeof(ElemArgs32) * n, cudaMemcpyHostToDevice));
+  }
+  return EQD_OK;
+}
+
+int launch_elements_batched(const void *handle, cudaStream_t s, int part) {
+  const ElemBatch *b = static_cast<const ElemBatch *>(handle);
+  for (int grp = 0; grp < 2; ++grp) {
+    if ((grp == 0 && part == 1) || (grp == 1 && part == 0) || b->tiles[grp] == 0) continue;
+    const int rc = b->v.hg == 2
+                       ? launch_batched_hg<2>(b->v, grp == 0, b->d_args[grp], b->d_start[grp], b->n, b->tiles[grp],
+                                              b->Mmax[grp], s)
+                       : launch_batched_hg<1>(b->v, grp == 0, b->d_args[grp], b->d_start[grp], b->n, b->tiles[grp],
+                                              b->Mmax[grp], s);
+    if (rc) return rc;
+  }
+  return cudaGetLastError() == cudaSuccess ? EQD_OK : EQD_ERR_CUDA;
+}
+
+void elem_batch_free(void *handle) {
+  ElemBatch *b = static_cast<ElemBatch *>(handle);
+  if (!b) return;
+  for (int grp = 0; grp < 2; ++grp) {
+    if (b->d_args[grp]) cudaFree(b->d_args[grp]);
+    if (b->d_start[grp]) cudaFree(b->d_start[grp]);
+  }
+  delete b;
 }
 
 }  // namespace eqd

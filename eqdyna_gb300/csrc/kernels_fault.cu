@@ -7,6 +7,8 @@
 // fault_kernel : one thread per split-node pair: thermop (src/thermop.f90), faulting
 //                (src/faulting.f90:3-541) with the friction laws (src/fric.f90), station capture
 //                (src/faulting.f90:518-541, src/driver.f90:157-180) and rupture time.
+#include <vector>
+
 #include "eqd_device.cuh"
 #include "mlp_common.cuh"
 #include "rsf_newton.cuh"
@@ -15,13 +17,14 @@ namespace eqd {
 
 namespace {
 
-constexpr int kBlockNode = 256;
-constexpr int kBlockFault = 128;
+constexpr int kBlockNode = 256;       // default node-update block
+constexpr int kBlockNodeMax = 512;
+constexpr int kBlockFault = 128;      // default and largest fault-kernel block
 
 // COPY32: also writes the binary32 copies of velocity and of u + rdampk v read by the binary32
 // element kernels (the binary64 arrays stay the state).
 template <bool F_IS_ACC, bool COPY32>
-__global__ void __launch_bounds__(kBlockNode)
+__global__ void __launch_bounds__(kBlockNodeMax)
     node_update(double *__restrict__ vel, double *__restrict__ disp, double *__restrict__ F,
                 const double *__restrict__ inv_mass, double *__restrict__ F9,
                 double *__restrict__ v9, double *__restrict__ vh,
@@ -90,22 +93,48 @@ __global__ void __launch_bounds__(kBlockNode)
   if (isnan(v[0]) || isnan(v[1]) || isnan(v[2])) atomicOr(d_err, 1);
 }
 
+// Arguments of the binary32 node update (one context).
+struct NodeArgs32 {
+  double *vel, *disp;
+  float *F;
+  const float *inv_mass;
+  float *F9, *v9;
+  double *vh;
+  const float *pml_ab;
+  int nnode, n_int, npml, nsplit;
+  float dt;
+  double dtd, rdampk;
+  int *d_nt, *d_err;
+  float *vel32, *dl32;
+  const double *Fsplit;
+  const int *split_slot;
+  int f_is_acc;  // used by the batched launch (the single launch selects a template instead)
+};
+
 // Node update of the binary32 form.  The force sums arrive in binary32 (Kahan-compensated per
 // tile); acceleration, its increment a*dt and the PML split-field velocities are binary32, while
 // velocity and displacement of every node stay binary64 (increments are small against the state,
 // which is accumulated over 10^3 - 10^4 steps).  About 6 binary64 operations per component.
 // Split (fault) nodes are updated entirely in binary64.
 template <bool F_IS_ACC>
-__global__ void __launch_bounds__(kBlockNode)
-    node_update32(double *__restrict__ vel, double *__restrict__ disp, float *__restrict__ F,
-                  const float *__restrict__ inv_mass, float *__restrict__ F9,
-                  float *__restrict__ v9, double *__restrict__ vh,
-                  const float *__restrict__ pml_ab, int nnode, int n_int, int npml, float dt,
-                  double dtd, int *__restrict__ d_nt, int *__restrict__ d_err,
-                  float *__restrict__ vel32, float *__restrict__ dl32, double rdampk,
-                  const double *__restrict__ Fsplit, const int *__restrict__ split_slot, int nsplit) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i == 0) *d_nt += 1;
+__device__ __forceinline__ void node_update32_body(const NodeArgs32 &a, int i) {
+  double *__restrict__ vel = a.vel;
+  double *__restrict__ disp = a.disp;
+  float *__restrict__ F = a.F;
+  const float *__restrict__ inv_mass = a.inv_mass;
+  float *__restrict__ F9 = a.F9;
+  float *__restrict__ v9 = a.v9;
+  double *__restrict__ vh = a.vh;
+  const float *__restrict__ pml_ab = a.pml_ab;
+  const int nnode = a.nnode, n_int = a.n_int, npml = a.npml, nsplit = a.nsplit;
+  const float dt = a.dt;
+  const double dtd = a.dtd, rdampk = a.rdampk;
+  int *__restrict__ d_err = a.d_err;
+  float *__restrict__ vel32 = a.vel32;
+  float *__restrict__ dl32 = a.dl32;
+  const double *__restrict__ Fsplit = a.Fsplit;
+  const int *__restrict__ split_slot = a.split_slot;
+  if (i == 0) *a.d_nt += 1;
   if (i >= nnode) return;
   const float im = inv_mass[i];
   double v[3];
@@ -184,6 +213,38 @@ __global__ void __launch_bounds__(kBlockNode)
   if (isnan(v[0]) || isnan(v[1]) || isnan(v[2])) atomicOr(d_err, 1);
 }
 
+template <bool F_IS_ACC>
+__global__ void __launch_bounds__(kBlockNodeMax) node_update32(NodeArgs32 a) {
+  node_update32_body<F_IS_ACC>(a, blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+// Member of a batch that owns block b: the largest m with start[m] <= b (start: n + 1 prefix sums).
+__device__ __forceinline__ int batch_member(const int *__restrict__ start, int n, int b) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (start[mid] <= b) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+// Node update of every member of an ensemble in one launch.
+__global__ void __launch_bounds__(kBlockNode) node_update32_batched(const NodeArgs32 *__restrict__ args,
+                                                                    const int *__restrict__ start, int n) {
+  __shared__ NodeArgs32 a;
+  __shared__ int lb;
+  if (threadIdx.x == 0) {
+    const int m = batch_member(start, n, blockIdx.x);
+    a = args[m];
+    lb = blockIdx.x - start[m];
+  }
+  __syncthreads();
+  const int i = lb * blockDim.x + threadIdx.x;
+  if (a.f_is_acc) node_update32_body<true>(a, i);
+  else node_update32_body<false>(a, i);
+}
+
 struct FaultArgs {
   int npair, nnode, nstep, nOnSt, nOffRows, nftmx_tp;
   int friclaw, TPV, C_nuclea_here, C_elastic, insertFaultType;
@@ -222,12 +283,56 @@ __device__ __forceinline__ void force_set(const FaultArgs &p, int c, int node, i
   else p.F[(size_t)c * p.nnode + node] = v;
 }
 
+// Thermal pressurization (src/thermop.f90:1-40): pore pressure and temperature change of every
+// pair by convolution of its slip-rate x shear-stress history with the diffusion kernels, O(nt)
+// per pair per step.  32 pairs per CTA of 8 warps; warp w takes history rows w, w + 8, ... (each
+// row a coalesced 32-pair read of the step-major history), the warps' partial sums are added in
+// shared memory.
+constexpr int kTpWarps = 8;
+__global__ void __launch_bounds__(32 * kTpWarps) thermop_kernel(FaultArgs p) {
+  __shared__ double part[kTpWarps][2][32];
+  const int nt = *p.d_nt;
+  const int np = p.npair;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int i = blockIdx.x * 32 + lane;
+  double tp = 0.0, tt = 0.0;
+  if (i < np) {
+    const double *fr = p.fric + i;
+#define FR(k) fr[((k)-1) * np]
+    const double omega = FR(16), kapa = FR(17), h2 = 2.0 * p.fric_tp_h * p.fric_tp_h;
+    const double dt = p.dt;
+    const int jmax = nt - 1 < p.nstep ? nt - 1 : p.nstep;  // history rows that exist
+    for (int j = 1 + w; j <= jmax; j += kTpWarps) {
+      const double *hh = p.tp_hist + 2 * ((size_t)i + (size_t)np * (j - 1));
+      const double q = fabs(hh[1]) * hh[0];
+      const double s1 = sqrt(4.0 * kapa * (nt - j) * dt + h2);
+      const double s2 = sqrt(4.0 * omega * (nt - j) * dt + h2);
+      const double ker = -kapa / (omega - kapa) / s1 + omega / (omega - kapa) / s2;
+      tp += q * ker * dt;
+      tt += q * (1.0 / s1) * dt;
+    }
+#undef FR
+  }
+  part[w][0][lane] = tp;
+  part[w][1][lane] = tt;
+  __syncthreads();
+  if (w == 0 && i < np) {
+    for (int k = 1; k < kTpWarps; ++k) tp += part[k][0][lane], tt += part[k][1][lane];
+    double *fr = p.fric + i;
+#define FR(k) fr[((k)-1) * np]
+    const double gama = FR(19) / FR(18);
+    const double rpi = sqrt(3.14159265358979323846);
+    FR(51) = tp * gama / rpi;
+    FR(52) = tt / FR(18) / rpi + FR(41);
+#undef FR
+  }
+}
+
 template <bool F32>
-__global__ void __launch_bounds__(kBlockFault) fault_kernel(FaultArgs p) {
-  __shared__ __align__(16) __nv_bfloat16 mlp_xs[kBlockFault / 32][32 * kMlpK1];
+__device__ __forceinline__ void fault_body(const FaultArgs &p, int tid,
+                                           __nv_bfloat16 (*mlp_xs)[32 * kMlpK1]) {
   const int nt = *p.d_nt;
   const double t = p.d_times[nt];
-  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   const int np = p.npair;
   const int nn = p.nnode;
   if (tid >= np) {
@@ -255,24 +360,8 @@ __global__ void __launch_bounds__(kBlockFault) fault_kernel(FaultArgs p) {
   const double arn = p.geo[9 * np + i], mS = p.geo[10 * np + i], mM = p.geo[11 * np + i];
   const double radius = p.geo[12 * np + i];
 
-  // thermal pressurization (src/thermop.f90) — uses the history of previous steps
-  if (p.friclaw == 5 && p.tp_hist) {
-    const double gama = FR(19) / FR(18), omega = FR(16), kapa = FR(17), h2 = 2.0 * p.fric_tp_h * p.fric_tp_h;
-    double tp = 0.0, tt = 0.0;
-    const int jmax = nt - 1 < p.nstep ? nt - 1 : p.nstep;  // history rows that exist
-    for (int j = 1; j <= jmax; ++j) {
-      const double *hh = p.tp_hist + 2 * ((size_t)i + (size_t)np * (j - 1));
-      const double q = fabs(hh[1]) * hh[0];
-      const double s1 = sqrt(4.0 * kapa * (nt - j) * dt + h2);
-      const double s2 = sqrt(4.0 * omega * (nt - j) * dt + h2);
-      const double ker = -kapa / (omega - kapa) / s1 + omega / (omega - kapa) / s2;
-      tp += q * ker * dt;
-      tt += q * (1.0 / s1) * dt;
-    }
-    const double rpi = sqrt(3.14159265358979323846);
-    FR(51) = tp * gama / rpi;
-    FR(52) = tt / FR(18) / rpi + FR(41);
-  }
+  // thermal pressurization (src/thermop.f90): fric(51), fric(52) come from thermop_kernel, which
+  // runs just before this kernel
 
   // getNsdSlipSliprateTraction (src/faulting.f90:54-134)
   const double init[3] = {FR(7), FR(8), FR(49)};
@@ -501,30 +590,55 @@ __global__ void __launch_bounds__(kBlockFault) fault_kernel(FaultArgs p) {
 #undef FR
 }
 
-}  // namespace
-
-int launch_node_update(Context &c, cudaStream_t s) {
-  const int grid = (c.nnode + kBlockNode - 1) / kBlockNode;
-#define EQD_NODE_ARGS c.vel, c.disp, c.F, c.inv_mass, c.F9, c.v9, c.vh, c.pml_ab, c.nnode, c.n_int, \
-    c.npml, c.sc.dt, c.d_nt, c.d_err, c.vel32, c.dl32, c.sc.rdampk
-  if (c.fp32) {
-#define EQD_NODE32_ARGS c.vel, c.disp, c.F32, c.inv_mass32, c.F9_32, c.v9_32, c.vh, c.pml_ab32, c.nnode, \
-    c.n_int, c.npml, (float)c.sc.dt, c.sc.dt, c.d_nt, c.d_err, c.vel32, c.dl32, c.sc.rdampk, c.Fsplit, \
-    c.split_slot, 2 * c.npair
-    if (c.f_is_acc) node_update32<true><<<grid, kBlockNode, 0, s>>>(EQD_NODE32_ARGS);
-    else node_update32<false><<<grid, kBlockNode, 0, s>>>(EQD_NODE32_ARGS);
-#undef EQD_NODE32_ARGS
-  } else {
-    if (c.f_is_acc) node_update<true, false><<<grid, kBlockNode, 0, s>>>(EQD_NODE_ARGS);
-    else node_update<false, false><<<grid, kBlockNode, 0, s>>>(EQD_NODE_ARGS);
-  }
-#undef EQD_NODE_ARGS
-  return cudaGetLastError() == cudaSuccess ? EQD_OK : EQD_ERR_CUDA;
+template <bool F32>
+__global__ void __launch_bounds__(kBlockFault) fault_kernel(FaultArgs p) {
+  __shared__ __align__(16) __nv_bfloat16 mlp_xs[kBlockFault / 32][32 * kMlpK1];
+  fault_body<F32>(p, blockIdx.x * blockDim.x + threadIdx.x, mlp_xs);
 }
 
-int launch_fault(Context &c, cudaStream_t s) {
-  const int nthreads = c.npair + (c.nOffRows > 0 ? c.nOffRows + 1 : 0);
-  if (nthreads == 0) return EQD_OK;
+// Fault pairs (and station rows) of every member of an ensemble in one launch.
+__global__ void __launch_bounds__(kBlockFault) fault_kernel_batched(const FaultArgs *__restrict__ args,
+                                                                    const int *__restrict__ start, int n) {
+  __shared__ __align__(16) __nv_bfloat16 mlp_xs[kBlockFault / 32][32 * kMlpK1];
+  __shared__ FaultArgs p;
+  __shared__ int lb;
+  if (threadIdx.x == 0) {
+    const int m = batch_member(start, n, blockIdx.x);
+    p = args[m];
+    lb = blockIdx.x - start[m];
+  }
+  __syncthreads();
+  fault_body<true>(p, lb * blockDim.x + threadIdx.x, mlp_xs);
+}
+
+NodeArgs32 node_args32(const Context &c) {
+  NodeArgs32 a;
+  a.vel = c.vel;
+  a.disp = c.disp;
+  a.F = c.F32;
+  a.inv_mass = c.inv_mass32;
+  a.F9 = c.F9_32;
+  a.v9 = c.v9_32;
+  a.vh = c.vh;
+  a.pml_ab = c.pml_ab32;
+  a.nnode = c.nnode;
+  a.n_int = c.n_int;
+  a.npml = c.npml;
+  a.dt = (float)c.sc.dt;
+  a.dtd = c.sc.dt;
+  a.d_nt = c.d_nt;
+  a.d_err = c.d_err;
+  a.vel32 = c.vel32;
+  a.dl32 = c.dl32;
+  a.rdampk = c.sc.rdampk;
+  a.Fsplit = c.Fsplit;
+  a.split_slot = c.split_slot;
+  a.nsplit = 2 * c.npair;
+  a.f_is_acc = c.f_is_acc;
+  return a;
+}
+
+FaultArgs fault_args(Context &c) {
   FaultArgs p;
   p.npair = c.npair;
   p.nnode = c.nnode;
@@ -567,9 +681,111 @@ int launch_fault(Context &c, cudaStream_t s) {
   p.log_nt0 = c.nlog_nt0;
   p.log_steps = c.nlog_steps;
   p.log_stride = c.nlog_stride;
-  const int grid = (nthreads + kBlockFault - 1) / kBlockFault;
-  if (c.fp32) fault_kernel<true><<<grid, kBlockFault, 0, s>>>(p);
-  else fault_kernel<false><<<grid, kBlockFault, 0, s>>>(p);
+  return p;
+}
+
+}  // namespace
+
+int launch_node_update(Context &c, cudaStream_t s) {
+  const int bn = c.opt.block_node > 0 ? c.opt.block_node : kBlockNode;
+  const int grid = (c.nnode + bn - 1) / bn;
+#define EQD_NODE_ARGS c.vel, c.disp, c.F, c.inv_mass, c.F9, c.v9, c.vh, c.pml_ab, c.nnode, c.n_int, \
+    c.npml, c.sc.dt, c.d_nt, c.d_err, c.vel32, c.dl32, c.sc.rdampk
+  if (c.fp32) {
+    const NodeArgs32 a = node_args32(c);
+    if (c.f_is_acc) node_update32<true><<<grid, bn, 0, s>>>(a);
+    else node_update32<false><<<grid, bn, 0, s>>>(a);
+  } else {
+    if (c.f_is_acc) node_update<true, false><<<grid, bn, 0, s>>>(EQD_NODE_ARGS);
+    else node_update<false, false><<<grid, bn, 0, s>>>(EQD_NODE_ARGS);
+  }
+#undef EQD_NODE_ARGS
+  return cudaGetLastError() == cudaSuccess ? EQD_OK : EQD_ERR_CUDA;
+}
+
+namespace {
+struct NodeFaultBatch {
+  int n = 0;
+  NodeArgs32 *d_node = nullptr;
+  FaultArgs *d_fault = nullptr;
+  int *d_node_start = nullptr, *d_fault_start = nullptr;  // [n + 1] block prefix sums
+  int node_blocks = 0, fault_blocks = 0;
+  std::vector<NodeArgs32> h_node;
+  std::vector<FaultArgs> h_fault;
+};
+}  // namespace
+
+int node_fault_batch_update(void **handle, Context *const *m, int n) {
+  if (n <= 0) return EQD_ERR_INPUT;
+  for (int i = 0; i < n; ++i)
+    if (!m[i]->fp32 || (m[i]->sc.friclaw == 5 && m[i]->tp_hist)) return EQD_ERR_UNSUPPORTED;
+  NodeFaultBatch *b = static_cast<NodeFaultBatch *>(*handle);
+  if (!b) {
+    b = new NodeFaultBatch();
+    b->n = n;
+    std::vector<int> ns(n + 1, 0), fs(n + 1, 0);
+    for (int i = 0; i < n; ++i) {
+      ns[i + 1] = ns[i] + (m[i]->nnode + kBlockNode - 1) / kBlockNode;
+      const int nthreads = m[i]->npair + (m[i]->nOffRows > 0 ? m[i]->nOffRows + 1 : 0);
+      fs[i + 1] = fs[i] + (nthreads + kBlockFault - 1) / kBlockFault;
+    }
+    b->node_blocks = ns[n];
+    b->fault_blocks = fs[n];
+    if (cudaMalloc(&b->d_node, sizeof(NodeArgs32) * n) != cudaSuccess ||
+        cudaMalloc(&b->d_fault, sizeof(FaultArgs) * n) != cudaSuccess ||
+        cudaMalloc(&b->d_node_start, sizeof(int) * (n + 1)) != cudaSuccess ||
+        cudaMalloc(&b->d_fault_start, sizeof(int) * (n + 1)) != cudaSuccess) {
+      node_fault_batch_free(b);
+      return EQD_ERR_OOM;
+    }
+    cudaMemcpy(b->d_node_start, ns.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice);
+    cudaMemcpy(b->d_fault_start, fs.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice);
+    b->h_node.resize(n);
+    b->h_fault.resize(n);
+    *handle = b;
+  }
+  if (b->n != n) return EQD_ERR_INPUT;
+  for (int i = 0; i < n; ++i) {
+    b->h_node[i] = node_args32(*m[i]);
+    b->h_fault[i] = fault_args(*m[i]);
+  }
+  EQD_CUDA_OK(cudaMemcpy(b->d_node, b->h_node.data(), sizeof(NodeArgs32) * n, cudaMemcpyHostToDevice));
+  EQD_CUDA_OK(cudaMemcpy(b->d_fault, b->h_fault.data(), sizeof(FaultArgs) * n, cudaMemcpyHostToDevice));
+  return EQD_OK;
+}
+
+int launch_node_update_batched(const void *handle, cudaStream_t s) {
+  const NodeFaultBatch *b = static_cast<const NodeFaultBatch *>(handle);
+  if (b->node_blocks > 0) node_update32_batched<<<b->node_blocks, kBlockNode, 0, s>>>(b->d_node, b->d_node_start, b->n);
+  return cudaGetLastError() == cudaSuccess ? EQD_OK : EQD_ERR_CUDA;
+}
+
+int launch_fault_batched(const void *handle, cudaStream_t s) {
+  const NodeFaultBatch *b = static_cast<const NodeFaultBatch *>(handle);
+  if (b->fault_blocks > 0) fault_kernel_batched<<<b->fault_blocks, kBlockFault, 0, s>>>(b->d_fault, b->d_fault_start, b->n);
+  return cudaGetLastError() == cudaSuccess ? EQD_OK : EQD_ERR_CUDA;
+}
+
+void node_fault_batch_free(void *handle) {
+  NodeFaultBatch *b = static_cast<NodeFaultBatch *>(handle);
+  if (!b) return;
+  if (b->d_node) cudaFree(b->d_node);
+  if (b->d_fault) cudaFree(b->d_fault);
+  if (b->d_node_start) cudaFree(b->d_node_start);
+  if (b->d_fault_start) cudaFree(b->d_fault_start);
+  delete b;
+}
+
+int launch_fault(Context &c, cudaStream_t s) {
+  const int nthreads = c.npair + (c.nOffRows > 0 ? c.nOffRows + 1 : 0);
+  if (nthreads == 0) return EQD_OK;
+  const FaultArgs p = fault_args(c);
+  if (p.friclaw == 5 && p.tp_hist)
+    thermop_kernel<<<(c.npair + 31) / 32, 32 * kTpWarps, 0, s>>>(p);
+  const int bf = c.opt.block_fault > 0 ? c.opt.block_fault : kBlockFault;
+  const int grid = (nthreads + bf - 1) / bf;
+  if (c.fp32) fault_kernel<true><<<grid, bf, 0, s>>>(p);
+  else fault_kernel<false><<<grid, bf, 0, s>>>(p);
   return cudaGetLastError() == cudaSuccess ? EQD_OK : EQD_ERR_CUDA;
 }
 

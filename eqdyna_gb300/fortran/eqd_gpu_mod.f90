@@ -32,8 +32,8 @@ module eqd_gpu_mod
   end type
 
   type, bind(C) :: eqd_options
-    integer(c_int32_t) :: precision, learned_guess, record_tp_hist, block_elem
-    integer(c_int32_t) :: use_graph, device, table_layout, reserved
+    integer(c_int32_t) :: precision, learned_guess, record_tp_hist, tile_shape
+    integer(c_int32_t) :: use_graph, device, table_layout, block_node, block_fault, reserved
   end type
 
   interface

@@ -19,7 +19,7 @@ PRECISIONS = {"fp64": N.PREC_FP64, "fp32": N.PREC_FP32}
 
 class GpuSolver:
     def __init__(self, case, precision="fp64", learned_guess=False, use_graph=True, device=0,
-                 record_tp_hist=False, table_layout="auto"):
+                 record_tp_hist=False, table_layout="auto", tile_shape=0, block_node=0, block_fault=0):
         self.lib = N.gpu_lib()
         self.case = case
         self._ha = case.host_arrays()
@@ -30,6 +30,9 @@ class GpuSolver:
         opt.use_graph = int(bool(use_graph))
         opt.device = int(device)
         opt.table_layout = N.TABLE_LAYOUTS[table_layout]
+        opt.tile_shape = int(tile_shape)
+        opt.block_node = int(block_node)
+        opt.block_fault = int(block_fault)
         self._opt = opt
         h = C.c_void_p()
         rc = self.lib.eqd_gpu_init(C.byref(case.scalars), C.byref(self._ha), C.byref(opt), C.byref(h))
@@ -93,6 +96,20 @@ class GpuSolver:
         if rc != 0:
             raise N.EqdError(rc, "eqd_gpu_newton_counts")
         return dict(zip(["iterations", "ivmax_hits", "executed", "learned"], list(out)))
+
+    def fetch_fric_rows(self, rows, out):
+        """Copy fric rows (1-based) into out[len(rows)][npair] (e.g. a PinnedArray's array)."""
+        r = np.ascontiguousarray(rows, dtype=np.int32)
+        assert out.shape == (len(r), self.case.npair) and out.dtype == np.float64 and out.flags.c_contiguous
+        self._rc(self.lib.eqd_gpu_fetch_fric_rows(self._h, r.ctypes.data_as(N.c_int32_p), len(r),
+                                                  out.ctypes.data_as(N.c_double_p)), "eqd_gpu_fetch_fric_rows")
+
+    def init_times(self):
+        """Wall time (s) of the phases of eqd_gpu_init."""
+        ms = (C.c_double * 8)()
+        self._rc(self.lib.eqd_gpu_init_times(self._h, ms), "eqd_gpu_init_times")
+        names = ["nodes", "element_order", "element_tables", "tiles", "tables_upload", "fault_stations"]
+        return {n: round(ms[k] / 1e3, 3) for k, n in enumerate(names)}
 
     # ---- learned Newton initial guess ----
     def newton_log(self, nsteps, stride=1):
@@ -187,6 +204,39 @@ class GpuSolver:
             self.close()
         except Exception:
             pass
+
+
+class Ensemble:
+    """Several GpuSolver members (scenarios of any size and time step, binary32 form with
+    record-indexed tables) advanced together: one launch per kernel per step over all members."""
+
+    def __init__(self, solvers):
+        self.lib = N.gpu_lib()
+        self.solvers = list(solvers)
+        hs = (C.c_void_p * len(self.solvers))(*[s._h for s in self.solvers])
+        h = C.c_void_p()
+        rc = self.lib.eqd_ensemble_create(hs, len(self.solvers), C.byref(h))
+        if rc != 0:
+            raise N.EqdError(rc, "eqd_ensemble_create")
+        self._h = h
+
+    def step(self, nsteps=1):
+        rc = self.lib.eqd_ensemble_step(self._h, int(nsteps))
+        if rc != 0:
+            raise N.EqdError(rc, "eqd_ensemble_step")
+        for s in self.solvers:
+            s.nt += int(nsteps)
+
+    def close(self):
+        if self._h:
+            self.lib.eqd_ensemble_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
 
 
 def mlp_gradient(params, x, t, device=0):

@@ -126,10 +126,13 @@ typedef struct eqd_options {
   int32_t precision;      /* enum eqd_precision                                                */
   int32_t learned_guess;  /* 1: MLP initial guess for the rate-and-state Newton (friclaw 3/4)  */
   int32_t record_tp_hist; /* 1: keep onFaultTPHist on the device (forced on for friclaw 5)     */
-  int32_t block_elem;     /* element-kernel block size, 0 = autotuned default                  */
+  int32_t tile_shape;     /* binary32 element tiles: bricks of bx | by << 8 | bz << 16 elements
+                             (product 128), 0 = 4 x 8 x 4; chosen by eqdyna_gb300.autotune     */
   int32_t use_graph;      /* 1: capture the multi-step loop in a CUDA graph                    */
   int32_t device;         /* CUDA device ordinal                                               */
   int32_t table_layout;   /* enum eqd_table_layout (binary32 form only)                        */
+  int32_t block_node;     /* node-update block size: 64, 128, 256 or 512; 0 = 256                */
+  int32_t block_fault;    /* fault-kernel block size: 32, 64 or 128; 0 = 128                     */
   int32_t reserved;
 } eqd_options;
 
@@ -152,6 +155,17 @@ int eqd_gpu_fetch(eqd_context *ctx, eqd_host_arrays *a);
 
 /* Copies only the fault state (fric, fnft) back — the cheap per-step read of a result. */
 int eqd_gpu_fetch_fault(eqd_context *ctx, double *fric, double *fnft);
+
+/* No counterpart in the reference: the per-step read of a step's result without the rest of the
+ * fault state.  Copies fric(k, :) for the nrows 1-based row numbers k in rows[] into
+ * dst[nrows][npair] (pair index fastest), e.g. rows 71-76 = slip, slip rate and peak slip rate.
+ * dst may be pinned (eqd_host_alloc) for a direct DMA. */
+int eqd_gpu_fetch_fric_rows(eqd_context *ctx, const int32_t *rows, int32_t nrows, double *dst);
+
+/* Page-locked host memory for the buffers a host program exchanges with the device every step
+ * (cudaHostAlloc / cudaFreeHost); NULL or EQD_ERR_CUDA on failure. */
+void *eqd_host_alloc(int64_t bytes);
+int eqd_host_free(void *p);
 
 /* Frees all device memory of the context (before MPI_Finalize, src/eqdyna3d.f90:86). */
 int eqd_gpu_finalize(eqd_context *ctx);
@@ -226,6 +240,26 @@ int eqd_gpu_newton_replay(eqd_context *ctx, int32_t learned, int32_t fast, int64
  * kernel: x[n][6] normalised inputs, t[n] normalised targets (gradient checks). */
 int eqd_mlp_gradient(int32_t device, const float *params, const float *x, const float *t, int32_t n,
                      float *loss, float *grad);
+
+/* ---- ensembles -----------------------------------------------------------------------------
+ * No counterpart in the reference (one scenario per process there).  Several contexts created by
+ * eqd_gpu_init on the same device — rupture scenarios of any mesh size and time step — advance
+ * together: each step is one launch per kernel over all members (node update, interior and PML
+ * elements, fault), captured in CUDA graphs.  Members must use the binary32 form with
+ * record-indexed element tables (table_layout AUTO resolving to records, or RECORDS) and share the
+ * physics switches (elastic/plastic, hourglass form, friction law other than 5).  Members keep their
+ * own state: eqd_gpu_fetch* work on each; do not step a member by itself while it is in an
+ * ensemble. */
+typedef struct eqd_ensemble eqd_ensemble;
+int eqd_ensemble_create(eqd_context *const *members, int32_t n, eqd_ensemble **ens);
+/* Advances every member by nsteps steps (each from its own current step). */
+int eqd_ensemble_step(eqd_ensemble *ens, int32_t nsteps);
+int eqd_ensemble_destroy(eqd_ensemble *ens);
+
+/* Wall time (ms) of the phases of eqd_gpu_init: 0 nodes (and the device context), 1 element
+ * grouping and ordering, 2 element tables, 3 binary32 tiles, 4 binary32 tables and element uploads,
+ * 5 fault and stations, 6-7 unused. */
+int eqd_gpu_init_times(eqd_context *ctx, double ms[8]);
 
 /* Element-table layout of the binary32 form for group 0 (interior) or 1 (PML):
  * info[0] = 2 record-indexed, 1 streamed, 0 group empty or binary64 form; info[1] = elements;

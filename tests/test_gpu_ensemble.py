@@ -1,0 +1,77 @@
+"""Ensembles: scenarios of different mesh sizes and time steps advanced together (one launch per
+kernel per step over all members) agree with each member run alone.
+
+Binary32 runs are not bitwise reproducible (the nodal sums end in binary32 L2 reductions from
+several CTAs), so members are compared with their solo runs to relative 1e-4.
+"""
+import tempfile
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+SCALES = (4.0, 5.0, 6.0)  # C0 generator at dx = 800, 1000, 1200 m; dt = 0.032, 0.040, 0.048 s
+NSTEPS = 60
+
+
+def _cases():
+    from eqdyna_gb300.case import Case
+    from eqdyna_gb300.configs import config_c0
+    return [Case.from_dir(config_c0(tempfile.mkdtemp(prefix="eqd_c0_"), scale=sc, nsteps=NSTEPS))
+            for sc in SCALES]
+
+
+def _rel(a, b):
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+def test_ensemble_matches_members_run_alone():
+    from eqdyna_gb300.solver import Ensemble, GpuSolver
+    cases = _cases()
+    assert len({c.sizes["nelem"] for c in cases}) == len(cases)
+    solo = []
+    for c in cases:
+        g = c.clone()
+        with GpuSolver(g, precision="fp32", table_layout="records") as s:
+            s.step(NSTEPS)
+            s.fetch()
+        solo.append(g)
+    members = [c.clone() for c in cases]
+    solvers = [GpuSolver(g, precision="fp32", table_layout="records") for g in members]
+    try:
+        with Ensemble(solvers) as e:
+            e.step(1)    # first step of every member (stored acceleration)
+            e.step(40)   # two captured 16-step graphs and a tail
+            e.step(NSTEPS - 41)
+        for s in solvers:
+            s.fetch()
+    finally:
+        for s in solvers:
+            s.close()
+    for c, a, b in zip(cases, members, solo):
+        fa, fb = a.fric(), b.fric()
+        rep = {"slip": _rel(fa[:, 70:73], fb[:, 70:73]), "slip_rate": _rel(fa[:, 73:76], fb[:, 73:76]),
+               "vel": _rel(a.arrays["velArr"], b.arrays["velArr"]),
+               "disp": _rel(a.arrays["dispArr"], b.arrays["dispArr"])}
+        print(c.sizes["nelem"], rep)
+        assert all(v <= 1e-4 for v in rep.values()), rep
+        ta, tb = a.arrays["fnft"][: a.npair], b.arrays["fnft"][: b.npair]
+        assert np.array_equal(ta < 1e4, tb < 1e4)
+        both = ta < 1e4
+        assert np.all(np.abs(ta[both] - tb[both]) <= c.scalars.dt * 1.000001)
+        assert np.abs(fa[:, 75]).max() > 0.0  # the rupture is under way
+
+
+def test_ensemble_rejects_streamed_members():
+    from eqdyna_gb300 import _native as N
+    from eqdyna_gb300.solver import Ensemble, GpuSolver
+    cases = _cases()[:2]
+    solvers = [GpuSolver(c.clone(), precision="fp32", table_layout="streamed") for c in cases]
+    try:
+        with pytest.raises(N.EqdError) as ei:
+            Ensemble(solvers)
+        assert ei.value.code == 5
+    finally:
+        for s in solvers:
+            s.close()
