@@ -1,7 +1,8 @@
 """In-tree build of the native libraries (no cmake, no setup.py).
 
   eqdyna_gb300/lib/libeqd_case.so     host case setup (g++)
-  eqdyna_gb300/lib/libeqdyna_gb300.so GB300 hot path + C ABI (nvcc, sm_103a only)
+  eqdyna_gb300/lib/libeqdyna_gb300.so GB300 hot path + C ABI (nvcc, sm_103a only; host setup
+                                      loops in OpenMP)
   oracle/liboracle.so                 CPU binary64 restatement used only by tests and the CPU
                                       baseline (g++ -fopenmp)
 
@@ -79,7 +80,7 @@ def build_gpu(force=False, verbose_ptxas=False, jobs=None):
         objs.append(obj)
         if force or _newer(obj, [src] + headers):
             cmd = [NVCC, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
-                   "-Xcompiler", "-ffp-contract=off", "-I" + INCLUDE, "-I" + CSRC,
+                   "-Xcompiler", "-ffp-contract=off", "-Xcompiler", "-fopenmp", "-I" + INCLUDE, "-I" + CSRC,
                    "-c", src, "-o", obj]
             if verbose_ptxas:
                 cmd += ["-Xptxas", "-v"]
@@ -89,7 +90,7 @@ def build_gpu(force=False, verbose_ptxas=False, jobs=None):
         with cf.ThreadPoolExecutor(max_workers=jobs or min(len(todo), os.cpu_count() or 4)) as ex:
             out = list(ex.map(_run, todo))
     if force or todo or _newer(GPU_LIB, objs):
-        _run([NVCC, *ARCH, "-shared", *objs, "-o", GPU_LIB, "-lcudart"])
+        _run([NVCC, *ARCH, "-shared", *objs, "-o", GPU_LIB, "-lcudart", "-lgomp"])
     return GPU_LIB, "".join(out)
 
 

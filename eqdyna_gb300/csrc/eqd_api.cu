@@ -10,6 +10,9 @@
 #include "eqd_device.cuh"
 #include "mlp_common.cuh"
 
+#include <omp.h>
+#include <parallel/algorithm>
+
 #include <algorithm>
 #include <chrono>
 #include <tuple>
@@ -121,7 +124,8 @@ void brick_order(const eqd_host_arrays &a, std::vector<int> &ids, int bx, int bz
   const size_t m = ids.size();
   if (m == 0) return;
   std::vector<double> c(3 * m), ext(3 * m);
-  double lo[3] = {1e300, 1e300, 1e300};
+  double lo0 = 1e300, lo1 = 1e300, lo2 = 1e300;
+#pragma omp parallel for schedule(static) reduction(min : lo0, lo1, lo2)
   for (size_t i = 0; i < m; ++i) {
     double mn[3] = {1e300, 1e300, 1e300}, mx[3] = {-1e300, -1e300, -1e300}, sum[3] = {0, 0, 0};
     for (int q = 0; q < 8; ++q) {
@@ -135,9 +139,12 @@ void brick_order(const eqd_host_arrays &a, std::vector<int> &ids, int bx, int bz
     for (int k = 0; k < 3; ++k) {
       c[3 * i + k] = sum[k] / 8.0;
       ext[3 * i + k] = mx[k] - mn[k];
-      lo[k] = std::min(lo[k], c[3 * i + k]);
     }
+    lo0 = std::min(lo0, c[3 * i]);
+    lo1 = std::min(lo1, c[3 * i + 1]);
+    lo2 = std::min(lo2, c[3 * i + 2]);
   }
+  const double lo[3] = {lo0, lo1, lo2};
   double h[3];
   for (int k = 0; k < 3; ++k) {
     std::vector<double> e(m);
@@ -147,13 +154,15 @@ void brick_order(const eqd_host_arrays &a, std::vector<int> &ids, int bx, int bz
   }
   using Key = std::tuple<long, long, long, long, long, long, int>;
   std::vector<Key> keys(m);
+#pragma omp parallel for schedule(static)
   for (size_t i = 0; i < m; ++i) {
     const long fx = (long)std::floor((c[3 * i] - lo[0]) / h[0] + 0.5);
     const long fy = (long)std::floor((c[3 * i + 1] - lo[1]) / h[1] + 0.5);
     const long fz = (long)std::floor((c[3 * i + 2] - lo[2]) / h[2] + 0.5);
     keys[i] = Key(fx / bx, fz / bz, fy / by, fx, fz, fy, ids[i]);
   }
-  std::sort(keys.begin(), keys.end());
+  __gnu_parallel::sort(keys.begin(), keys.end());
+#pragma omp parallel for schedule(static)
   for (size_t i = 0; i < m; ++i) ids[i] = std::get<6>(keys[i]);
 }
 
@@ -164,13 +173,16 @@ int build_tiles(Context &c, ElemGroup<float> &g, const std::vector<int> &conn_de
   const int m = g.ne;
   g.tile = tile;
   g.ntiles = (m + tile - 1) / tile;
-  std::vector<int> node_ptr(1, 0), nodes, incp_off(1, 0);
-  std::vector<unsigned short> incp, inc((size_t)g.ntiles * tile * 8, 0);
-  std::vector<std::pair<int, int>> pairs;
+  const int nt = g.ntiles;
+  std::vector<unsigned short> inc((size_t)nt * tile * 8, 0);
+  std::vector<std::vector<int>> tnodes(nt);
+  std::vector<std::vector<unsigned short>> tincp(nt);
   int maxM = 0;
-  for (int t = 0; t < g.ntiles; ++t) {
+#pragma omp parallel for schedule(dynamic, 64) reduction(max : maxM)
+  for (int t = 0; t < nt; ++t) {
     const int e0 = t * tile, e1 = std::min(m, e0 + tile);
-    pairs.clear();
+    std::vector<std::pair<int, int>> pairs;
+    pairs.reserve((size_t)(e1 - e0) * 8);
     for (int e = e0; e < e1; ++e)
       for (int q = 0; q < 8; ++q) pairs.push_back({conn_dev[(size_t)q * m + e], q * tile + (e - e0)});
     std::sort(pairs.begin(), pairs.end());
@@ -181,19 +193,31 @@ int build_tiles(Context &c, ElemGroup<float> &g, const std::vector<int> &conn_de
     std::stable_sort(runs.begin(), runs.end(), [](const std::pair<size_t, size_t> &x, const std::pair<size_t, size_t> &y) {
       return x.second - x.first > y.second - y.first;
     });
-    int M = 0;
     const size_t base = (size_t)t * tile * 8;
+    std::vector<int> &nodes = tnodes[t];
+    std::vector<unsigned short> &incp = tincp[t];
+    nodes.reserve(runs.size());
+    incp.reserve(runs.size() + 1);
     size_t k = 0;
     for (const auto &run : runs) {
       nodes.push_back(pairs[run.first].first);
       incp.push_back((unsigned short)k);
-      ++M;
       for (size_t q = run.first; q < run.second; ++q) inc[base + k++] = (unsigned short)pairs[q].second;
     }
     incp.push_back((unsigned short)pairs.size());
-    node_ptr.push_back((int)nodes.size());
-    incp_off.push_back((int)incp.size());
-    maxM = std::max(maxM, M);
+    maxM = std::max(maxM, (int)runs.size());
+  }
+  std::vector<int> node_ptr(nt + 1, 0), incp_off(nt + 1, 0);
+  for (int t = 0; t < nt; ++t) {
+    node_ptr[t + 1] = node_ptr[t] + (int)tnodes[t].size();
+    incp_off[t + 1] = incp_off[t] + (int)tincp[t].size();
+  }
+  std::vector<int> nodes(node_ptr[nt]);
+  std::vector<unsigned short> incp(incp_off[nt]);
+#pragma omp parallel for schedule(static)
+  for (int t = 0; t < nt; ++t) {
+    std::copy(tnodes[t].begin(), tnodes[t].end(), nodes.begin() + node_ptr[t]);
+    std::copy(tincp[t].begin(), tincp[t].end(), incp.begin() + incp_off[t]);
   }
   g.max_tile_nodes = std::max(maxM, 1);
   int rc;
@@ -205,7 +229,12 @@ int build_tiles(Context &c, ElemGroup<float> &g, const std::vector<int> &conn_de
   return EQD_OK;
 }
 
-std::vector<float> to_f32(const std::vector<double> &v) { return std::vector<float>(v.begin(), v.end()); }
+std::vector<float> to_f32(const std::vector<double> &v) {
+  std::vector<float> out(v.size());
+#pragma omp parallel for schedule(static)
+  for (long long i = 0; i < (long long)v.size(); ++i) out[i] = (float)v[i];
+  return out;
+}
 
 // Distinct binary32 element records: open addressing over a 64-bit hash of the record's bits.
 class RecordDict {
@@ -267,8 +296,11 @@ constexpr long kAutoMaxRecords = 65536;
 std::vector<float> to_f32_rows(const std::vector<double> &v, size_t m, size_t ld) {
   const size_t nc = v.size() / m;
   std::vector<float> out(nc * ld, 0.f);
-  for (size_t q = 0; q < nc; ++q)
-    for (size_t i = 0; i < m; ++i) out[q * ld + i] = (float)v[q * m + i];
+#pragma omp parallel for schedule(static)
+  for (long long qi = 0; qi < (long long)(nc * m); ++qi) {
+    const size_t q = (size_t)qi / m, i = (size_t)qi % m;
+    out[q * ld + i] = (float)v[qi];
+  }
   return out;
 }
 
@@ -322,54 +354,64 @@ int build_device_state(eqd_context &X, const eqd_scalars &s, const eqd_host_arra
   std::vector<double> vel(3 * (size_t)nn), disp(3 * (size_t)nn), F(3 * (size_t)nn, 0.0), inv_mass(nn, 0.0);
   std::vector<double> F9(9 * (size_t)np_, 0.0), v9(9 * (size_t)np_, 0.0), vh(3 * (size_t)np_, 0.0);
   std::vector<double> pml_ab(6 * (size_t)np_, 0.0);
+  int bad_ = EQD_OK;
+#pragma omp parallel for schedule(static)
   for (int d = 0; d < nn; ++d) {
-    const int j = X.node_orig[d], node = j + 1;
-    for (int k = 0; k < 3; ++k) disp[k * (size_t)nn + d] = a.dispArr[3 * (size_t)j + k];
-    if (d < c.n_int) {
-      double m = -1;
-      for (int k = 1; k <= 3; ++k) {
-        const int e = eq(node, k);
-        if (e < 1 || e > a.neq) return EQD_ERR_UNSUPPORTED;  // fixed 3-DOF node: not built
-        const double mk = a.nodalMassArr[e - 1];
-        if (k == 1) m = mk;
-        else if (mk != m) return EQD_ERR_UNSUPPORTED;  // anisotropic lumped mass: not built
-        vel[(k - 1) * (size_t)nn + d] = a.v1[e - 1];
-        F[(k - 1) * (size_t)nn + d] = a.nodalForceArr[e - 1];
-      }
-      if (!(m > 0)) return EQD_ERR_INPUT;
-      inv_mass[d] = 1.0 / m;
-    } else {
-      const int p = d - c.n_int;
-      for (int k = 0; k < 3; ++k) vel[k * (size_t)nn + d] = a.velArr[3 * (size_t)j + k];
-      const int e1 = eq(node, 1);
-      if (e1 > 0) {
-        const double m = a.nodalMassArr[e1 - 1];
-        if (!(m > 0)) return EQD_ERR_INPUT;
-        for (int k = 1; k <= 12; ++k) {
+    const int r_ = [&]() -> int {
+      const int j = X.node_orig[d], node = j + 1;
+      for (int k = 0; k < 3; ++k) disp[k * (size_t)nn + d] = a.dispArr[3 * (size_t)j + k];
+      if (d < c.n_int) {
+        double m = -1;
+        for (int k = 1; k <= 3; ++k) {
           const int e = eq(node, k);
-          if (e < 1 || e > a.neq) return EQD_ERR_UNSUPPORTED;
-          if (a.nodalMassArr[e - 1] != m) return EQD_ERR_UNSUPPORTED;
-          if (k <= 9) {
-            v9[(k - 1) * (size_t)np_ + p] = a.v1[e - 1];
-            F9[(k - 1) * (size_t)np_ + p] = a.nodalForceArr[e - 1];
-          } else {
-            vh[(k - 10) * (size_t)np_ + p] = a.v1[e - 1];
-            F[(k - 10) * (size_t)nn + d] = a.nodalForceArr[e - 1];
-          }
+          if (e < 1 || e > a.neq) return EQD_ERR_UNSUPPORTED;  // fixed 3-DOF node: not built
+          const double mk = a.nodalMassArr[e - 1];
+          if (k == 1) m = mk;
+          else if (mk != m) return EQD_ERR_UNSUPPORTED;  // anisotropic lumped mass: not built
+          vel[(k - 1) * (size_t)nn + d] = a.v1[e - 1];
+          F[(k - 1) * (size_t)nn + d] = a.nodalForceArr[e - 1];
         }
+        if (!(m > 0)) return EQD_ERR_INPUT;
         inv_mass[d] = 1.0 / m;
-        double dm[3];
-        pml_damping(s, a.meshCoor[3 * (size_t)j], a.meshCoor[3 * (size_t)j + 1], a.meshCoor[3 * (size_t)j + 2], false, dm);
-        for (int k = 0; k < 3; ++k) {
-          pml_ab[k * (size_t)np_ + p] = 1.0 / s.dt - dm[k] / 2.0;
-          pml_ab[(3 + k) * (size_t)np_ + p] = 1.0 / (1.0 / s.dt + dm[k] / 2.0);
-        }
       } else {
-        for (int k = 1; k <= 12; ++k)
-          if (eq(node, k) != -1) return EQD_ERR_UNSUPPORTED;  // partially fixed PML node
+        const int p = d - c.n_int;
+        for (int k = 0; k < 3; ++k) vel[k * (size_t)nn + d] = a.velArr[3 * (size_t)j + k];
+        const int e1 = eq(node, 1);
+        if (e1 > 0) {
+          const double m = a.nodalMassArr[e1 - 1];
+          if (!(m > 0)) return EQD_ERR_INPUT;
+          for (int k = 1; k <= 12; ++k) {
+            const int e = eq(node, k);
+            if (e < 1 || e > a.neq) return EQD_ERR_UNSUPPORTED;
+            if (a.nodalMassArr[e - 1] != m) return EQD_ERR_UNSUPPORTED;
+            if (k <= 9) {
+              v9[(k - 1) * (size_t)np_ + p] = a.v1[e - 1];
+              F9[(k - 1) * (size_t)np_ + p] = a.nodalForceArr[e - 1];
+            } else {
+              vh[(k - 10) * (size_t)np_ + p] = a.v1[e - 1];
+              F[(k - 10) * (size_t)nn + d] = a.nodalForceArr[e - 1];
+            }
+          }
+          inv_mass[d] = 1.0 / m;
+          double dm[3];
+          pml_damping(s, a.meshCoor[3 * (size_t)j], a.meshCoor[3 * (size_t)j + 1], a.meshCoor[3 * (size_t)j + 2], false, dm);
+          for (int k = 0; k < 3; ++k) {
+            pml_ab[k * (size_t)np_ + p] = 1.0 / s.dt - dm[k] / 2.0;
+            pml_ab[(3 + k) * (size_t)np_ + p] = 1.0 / (1.0 / s.dt + dm[k] / 2.0);
+          }
+        } else {
+          for (int k = 1; k <= 12; ++k)
+            if (eq(node, k) != -1) return EQD_ERR_UNSUPPORTED;  // partially fixed PML node
+        }
       }
+      return EQD_OK;
+    }();
+    if (r_) {
+#pragma omp critical(eqd_setup_status)
+      bad_ = r_;
     }
   }
+  if (bad_) return bad_;
   RC(dupload(c, c.vel, vel));
   RC(dupload(c, c.disp, disp));
   RC(dupload(c, c.inv_mass, inv_mass));
@@ -438,75 +480,87 @@ int build_device_state(eqd_context &X, const eqd_scalars &s, const eqd_host_arra
     const int nstress = grp == 0 ? (s.C_Q == 1 ? 12 : 6) : 15;
     std::vector<double> st(nstress * (size_t)m), st0, pab, em, hg, porep, pstr, qc;
     bool any_s0 = false;
+    int s0_any = 0;
     if (grp == 1) st0.assign(6 * (size_t)m, 0.0), pab.assign(6 * (size_t)m, 0.0);
     if (body) em.assign(8 * (size_t)m, 0.0);
     if (s.C_hg == 2) hg.assign(m, 0.0);
     if (grp == 0 && s.C_elastic == 0) porep.assign(m, 0.0), pstr.assign(m, 0.0);
     if (grp == 0 && s.C_Q == 1) qc.assign(5 * (size_t)m, 0.0);
+    int bad_ = EQD_OK;
+#pragma omp parallel for schedule(static) reduction(|| : s0_any)
     for (int i = 0; i < m; ++i) {
-      const int e = ids[i];
-      double ctr[3] = {0, 0, 0};
-      for (int q = 0; q < 8; ++q) {
-        const int node = a.nodeElemIdRelation[8 * (size_t)e + q];
-        if (node < 1 || node > nn) return EQD_ERR_INPUT;
-        conn[q * (size_t)m + i] = X.node_dev[node - 1];
-        for (int k = 0; k < 3; ++k) ctr[k] += a.meshCoor[3 * (size_t)(node - 1) + k];
-      }
-      for (double &v : ctr) v /= 8.0;
-      for (int q = 0; q < 24; ++q) shp[q * (size_t)m + i] = a.eleshp[24 * (size_t)e + q];
-      for (int q = 0; q < 32; ++q) phi[q * (size_t)m + i] = a.phi[32 * (size_t)e + q];
-      for (int q = 0; q < 6; ++q) ss[q * (size_t)m + i] = a.ss[6 * (size_t)e + q];
-      detw[i] = a.eledet[e] * s.w;
-      lam[i] = a.mat[3 * (size_t)ne + e];
-      mu[i] = a.mat[4 * (size_t)ne + e];
-      const int64_t base = a.stressCompIndexArr[e];
-      if (base < 0 || base + (grp == 0 ? nstress : 21) > a.size_stress) return EQD_ERR_INPUT;
-      for (int q = 0; q < nstress; ++q) st[q * (size_t)m + i] = a.stressArr[base + q];
-      if (grp == 1) {
-        for (int q = 0; q < 6; ++q) {
-          st0[q * (size_t)m + i] = a.stressArr[base + 15 + q];
-          any_s0 |= (st0[q * (size_t)m + i] != 0.0);
-        }
-        double dm[3];
-        pml_damping(s, ctr[0], ctr[1], ctr[2], true, dm);
-        for (int k = 0; k < 3; ++k) {
-          pab[k * (size_t)m + i] = 1.0 / s.dt - dm[k] / 2.0;
-          pab[(3 + k) * (size_t)m + i] = 1.0 / (1.0 / s.dt + dm[k] / 2.0);
-        }
-      }
-      if (body) {
-        if (!a.elemass) return EQD_ERR_INPUT;
+      const int r_ = [&]() -> int {
+        const int e = ids[i];
+        double ctr[3] = {0, 0, 0};
         for (int q = 0; q < 8; ++q) {
-          const double m0 = a.elemass[24 * (size_t)e + 3 * q];
-          if (a.elemass[24 * (size_t)e + 3 * q + 1] != m0 || a.elemass[24 * (size_t)e + 3 * q + 2] != m0)
-            return EQD_ERR_UNSUPPORTED;
-          em[q * (size_t)m + i] = m0;
+          const int node = a.nodeElemIdRelation[8 * (size_t)e + q];
+          if (node < 1 || node > nn) return EQD_ERR_INPUT;
+          conn[q * (size_t)m + i] = X.node_dev[node - 1];
+          for (int k = 0; k < 3; ++k) ctr[k] += a.meshCoor[3 * (size_t)(node - 1) + k];
         }
-      }
-      if (s.C_hg == 2)
-        hg[i] = 0.25 * s.kapa_hg * a.mat[2 * (size_t)ne + e] * a.mat[e] * std::pow(a.eledet[e] * s.w, 2.0 / 3.0);
-      if (grp == 0 && s.C_elastic == 0) {
-        porep[i] = a.eleporep ? a.eleporep[e] : 0.0;
-        pstr[i] = a.pstrain ? a.pstrain[e] : 0.0;
-      }
-      if (grp == 0 && s.C_Q == 1) {
-        // Q zone and mechanism index from the element centre (src/calcElemKU.f90:78-103)
-        const double Qs = ctr[2] > -1000.0 ? 10.0 : 50.0, Qp = 2.0 * Qs;
-        const int ip = (int)((ctr[0] - (s.PMLb[1] + s.dx / 2)) / s.dx + 1);
-        const int iq = (int)((ctr[1] - (s.PMLb[3] + s.dx / 2)) / s.dx + 1);
-        const int ir = (int)((ctr[2] - (s.PMLb[4] + s.dx / 2)) / s.dx + 1);
-        const int kk = 1 + ip % 2 + 2 * (iq % 2) + 4 * (ir % 2);
-        if (kk < 1 || kk > 8) return EQD_ERR_INPUT;
-        double tau, wkp, wks, cv, cs;
-        q_constants(Qp, kk, tau, wkp, cv);
-        q_constants(Qs, kk, tau, wks, cs);
-        qc[0 * (size_t)m + i] = std::exp(-s.dt / tau);
-        qc[1 * (size_t)m + i] = mu[i] * cs;
-        qc[2 * (size_t)m + i] = (lam[i] + 2 * mu[i]) * cv;
-        qc[3 * (size_t)m + i] = wkp * 8.0;
-        qc[4 * (size_t)m + i] = wks * 8.0;
+        for (double &v : ctr) v /= 8.0;
+        for (int q = 0; q < 24; ++q) shp[q * (size_t)m + i] = a.eleshp[24 * (size_t)e + q];
+        for (int q = 0; q < 32; ++q) phi[q * (size_t)m + i] = a.phi[32 * (size_t)e + q];
+        for (int q = 0; q < 6; ++q) ss[q * (size_t)m + i] = a.ss[6 * (size_t)e + q];
+        detw[i] = a.eledet[e] * s.w;
+        lam[i] = a.mat[3 * (size_t)ne + e];
+        mu[i] = a.mat[4 * (size_t)ne + e];
+        const int64_t base = a.stressCompIndexArr[e];
+        if (base < 0 || base + (grp == 0 ? nstress : 21) > a.size_stress) return EQD_ERR_INPUT;
+        for (int q = 0; q < nstress; ++q) st[q * (size_t)m + i] = a.stressArr[base + q];
+        if (grp == 1) {
+          for (int q = 0; q < 6; ++q) {
+            st0[q * (size_t)m + i] = a.stressArr[base + 15 + q];
+            s0_any |= (st0[q * (size_t)m + i] != 0.0);
+          }
+          double dm[3];
+          pml_damping(s, ctr[0], ctr[1], ctr[2], true, dm);
+          for (int k = 0; k < 3; ++k) {
+            pab[k * (size_t)m + i] = 1.0 / s.dt - dm[k] / 2.0;
+            pab[(3 + k) * (size_t)m + i] = 1.0 / (1.0 / s.dt + dm[k] / 2.0);
+          }
+        }
+        if (body) {
+          if (!a.elemass) return EQD_ERR_INPUT;
+          for (int q = 0; q < 8; ++q) {
+            const double m0 = a.elemass[24 * (size_t)e + 3 * q];
+            if (a.elemass[24 * (size_t)e + 3 * q + 1] != m0 || a.elemass[24 * (size_t)e + 3 * q + 2] != m0)
+              return EQD_ERR_UNSUPPORTED;
+            em[q * (size_t)m + i] = m0;
+          }
+        }
+        if (s.C_hg == 2)
+          hg[i] = 0.25 * s.kapa_hg * a.mat[2 * (size_t)ne + e] * a.mat[e] * std::pow(a.eledet[e] * s.w, 2.0 / 3.0);
+        if (grp == 0 && s.C_elastic == 0) {
+          porep[i] = a.eleporep ? a.eleporep[e] : 0.0;
+          pstr[i] = a.pstrain ? a.pstrain[e] : 0.0;
+        }
+        if (grp == 0 && s.C_Q == 1) {
+          // Q zone and mechanism index from the element centre (src/calcElemKU.f90:78-103)
+          const double Qs = ctr[2] > -1000.0 ? 10.0 : 50.0, Qp = 2.0 * Qs;
+          const int ip = (int)((ctr[0] - (s.PMLb[1] + s.dx / 2)) / s.dx + 1);
+          const int iq = (int)((ctr[1] - (s.PMLb[3] + s.dx / 2)) / s.dx + 1);
+          const int ir = (int)((ctr[2] - (s.PMLb[4] + s.dx / 2)) / s.dx + 1);
+          const int kk = 1 + ip % 2 + 2 * (iq % 2) + 4 * (ir % 2);
+          if (kk < 1 || kk > 8) return EQD_ERR_INPUT;
+          double tau, wkp, wks, cv, cs;
+          q_constants(Qp, kk, tau, wkp, cv);
+          q_constants(Qs, kk, tau, wks, cs);
+          qc[0 * (size_t)m + i] = std::exp(-s.dt / tau);
+          qc[1 * (size_t)m + i] = mu[i] * cs;
+          qc[2 * (size_t)m + i] = (lam[i] + 2 * mu[i]) * cv;
+          qc[3 * (size_t)m + i] = wkp * 8.0;
+          qc[4 * (size_t)m + i] = wks * 8.0;
+        }
+        return EQD_OK;
+      }();
+      if (r_) {
+#pragma omp critical(eqd_setup_status)
+        bad_ = r_;
       }
     }
+    if (bad_) return bad_;
+    any_s0 = s0_any;
     mark(2);
     if (c.fp32) {
       ElemGroup<float> &h = grp == 0 ? c.gi32 : c.gp32;
@@ -521,26 +575,53 @@ int build_device_state(eqd_context &X, const eqd_scalars &s, const eqd_host_arra
       std::vector<unsigned> rid, abid;
       std::vector<float> abt;
       if (use_rec) {
+        // per-thread dictionaries over contiguous chunks, merged in chunk order
         const long cap = layout == EQD_TABLES_RECORDS ? (long)m : std::min<long>(kAutoMaxRecords, m / 2 + 1);
         rid.assign(ld, 0u);
-        std::vector<float> r(dict.len(), 0.f);
-        for (int i = 0; i < m && use_rec; ++i) {
-          int q = 0;
-          for (int k = 0; k < 24; ++k) r[q++] = (float)shp[k * um + i];
-          if (s.C_hg == 2) {
-            r[q++] = (float)hg[i];
-          } else {
-            for (int k = 0; k < 32; ++k) r[q++] = (float)phi[k * um + i];
-            for (int k = 0; k < 6; ++k) r[q++] = (float)ss[k * um + i];
+        const int T = std::max(1, omp_get_max_threads());
+        std::vector<RecordDict> local(T, RecordDict(dict.len()));
+        std::vector<int> overflow(T, 0);
+#pragma omp parallel for schedule(static, 1) num_threads(T)
+        for (int t = 0; t < T; ++t) {
+          const long long i0 = (long long)m * t / T, i1 = (long long)m * (t + 1) / T;
+          std::vector<float> r(dict.len(), 0.f);
+          for (long long i = i0; i < i1; ++i) {
+            int q = 0;
+            for (int k = 0; k < 24; ++k) r[q++] = (float)shp[k * um + i];
+            if (s.C_hg == 2) {
+              r[q++] = (float)hg[i];
+            } else {
+              for (int k = 0; k < 32; ++k) r[q++] = (float)phi[k * um + i];
+              for (int k = 0; k < 6; ++k) r[q++] = (float)ss[k * um + i];
+            }
+            r[q++] = (float)detw[i];
+            r[q++] = (float)lam[i];
+            r[q++] = (float)mu[i];
+            if (body)
+              for (int k = 0; k < 8; ++k) r[q++] = (float)em[k * um + i];
+            const long id = local[t].find_or_add(r.data(), cap);
+            if (id < 0) {
+              overflow[t] = 1;
+              break;
+            }
+            rid[i] = (unsigned)id;
           }
-          r[q++] = (float)detw[i];
-          r[q++] = (float)lam[i];
-          r[q++] = (float)mu[i];
-          if (body)
-            for (int k = 0; k < 8; ++k) r[q++] = (float)em[k * um + i];
-          const long id = dict.find_or_add(r.data(), cap);
-          if (id < 0) use_rec = false;
-          else rid[i] = (unsigned)id;
+        }
+        std::vector<std::vector<unsigned>> to_global(T);
+        for (int t = 0; t < T && use_rec; ++t) {
+          if (overflow[t]) use_rec = false;
+          for (long j = 0; j < local[t].size() && use_rec; ++j) {
+            const long id = dict.find_or_add(local[t].rows().data() + (size_t)j * dict.len(), cap);
+            if (id < 0) use_rec = false;
+            else to_global[t].push_back((unsigned)id);
+          }
+        }
+        if (use_rec) {
+#pragma omp parallel for schedule(static, 1) num_threads(T)
+          for (int t = 0; t < T; ++t) {
+            const long long i0 = (long long)m * t / T, i1 = (long long)m * (t + 1) / T;
+            for (long long i = i0; i < i1; ++i) rid[i] = to_global[t][rid[i]];
+          }
         }
       }
       if (use_rec && grp == 1) {  // PML factors: distinct (a_k, b_k) per axis
