@@ -229,7 +229,12 @@ def bench_reference(args, world, rank):
     if rank != 0:
         return None
     with tempfile.TemporaryDirectory(prefix="eqd_bench_") as tmp:
-        case = build_case(args.config, args.scale, max(args.steps + args.warmup + 2, 10), tmp)
+        if args.config == "C4":  # one member of the ensemble (the oracle runs one scenario at a time)
+            from eqdyna_gb300.case import Case
+            from eqdyna_gb300.configs import config_c4
+            case = Case.from_dir(config_c4(tmp, 0, nsteps=max(args.steps + args.warmup + 2, 10)))
+        else:
+            case = build_case(args.config, args.scale, max(args.steps + args.warmup + 2, 10), tmp)
         from oracle import Oracle
         nth = os.cpu_count() or 1
         o = Oracle(case, nth)
@@ -419,6 +424,90 @@ def bench_ours(args, world, rank, local):
     return line if rank == 0 else None
 
 
+def bench_ensemble(args, world, rank, local):
+    """C4: an ensemble of members of different mesh sizes and time steps advanced together."""
+    import concurrent.futures as cf
+    import numpy as np
+    from eqdyna_gb300 import _native as N
+    from eqdyna_gb300.case import Case
+    from eqdyna_gb300.configs import WORKLOADS, config_c4
+    from eqdyna_gb300.solver import Ensemble, GpuSolver
+
+    job = args.job_steps if args.job_steps > 0 else 1500
+    nsteps = max(job, args.steps + args.warmup + 4)
+    t_setup = time.perf_counter()
+
+    def build(k):
+        d = tempfile.mkdtemp(prefix=f"eqd_c4_{k}_")
+        c = Case.from_dir(config_c4(d, k, nsteps=nsteps))
+        shutil.rmtree(d, ignore_errors=True)
+        return c
+    with cf.ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 4)) as ex:
+        cases = list(ex.map(build, range(args.members)))
+    setup_s = time.perf_counter() - t_setup
+    ne = [c.sizes["nelem"] for c in cases]
+    total = float(sum(ne))
+    dxs = {}
+    for c in cases:
+        dxs[str(int(round(c.scalars.dx)))] = dxs.get(str(int(round(c.scalars.dx))), 0) + 1
+
+    # ---- end to end: the whole ensemble job through the C ABI, every member's peak slip rate
+    # (fric row 76) read into pinned memory after every step ----
+    pinned = [N.PinnedArray((1, c.npair)) for c in cases]
+    barrier(world)
+    t0 = time.perf_counter()
+    solvers = [GpuSolver(c.clone(), precision="fp32", device=local) for c in cases]
+    ens = Ensemble(solvers)
+    t_init = time.perf_counter() - t0
+    for _ in range(job):
+        ens.step(1)
+        for sv, pa in zip(solvers, pinned):
+            sv.fetch_fric_rows([76], pa.array)
+    for sv in solvers:
+        sv.fetch()
+    e2e_s = time.perf_counter() - t0
+    ens.close()
+    for sv in solvers:
+        sv.close()
+    for pa in pinned:
+        pa.close()
+    e2e_s = allreduce_max(e2e_s, world)
+
+    # ---- device-timed steps ----
+    solvers = [GpuSolver(c.clone(), precision="fp32", device=local) for c in cases]
+    ens = Ensemble(solvers)
+    ens.step(args.warmup)
+    barrier(world)
+    with ClockSampler(local) as clk:
+        ens.step(args.steps)
+        dev_ms = ens.last_step_ms
+    barrier(world)
+    ens.close()
+    for sv in solvers:
+        sv.close()
+    dev_s = allreduce_max(dev_ms / 1e3, world)
+    units = allreduce_sum(total * args.steps, world)
+    value = units / dev_s
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dev_s * 1e3 / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 elements + f64 state",
+            "data": "synthetic (seeded config generator, no external dataset)",
+            "config": {"workload": f"C4: {WORKLOADS['C4']}", "members": args.members, "elements": int(total),
+                       "member_elements": [min(ne), max(ne)], "members_per_dx": dxs,
+                       "precision": "fp32", "parallelism": "replicas" if world > 1 else "single GPU",
+                       "l2": "inputs larger than L2, no flush", "setup_s": round(setup_s, 1)},
+            "e2e": {"value": total * job * world / e2e_s, "unit": UNIT, "steps": job,
+                    "init_s": round(t_init, 2),
+                    "h2d_bytes_per_step": int(sum(sum(v.nbytes for v in c.arrays.values() if v is not None)
+                                                  for c in cases) / job),
+                    "d2h_bytes_per_step": int(sum(c.npair for c in cases) * 8),
+                    "note": "whole ensemble job through the C ABI: init of every member, one ensemble step "
+                            "per call followed by a read of every member's peak slip rate into pinned "
+                            "memory, final fetch of every member"},
+            "gpu_launches": 4 * args.steps, "clocks": clk.summary()}
+    return line if rank == 0 else None
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -433,6 +522,7 @@ def main():
     ap.add_argument("--epochs", type=int, default=8)
     ap.add_argument("--job-steps", type=int, default=0, help="steps of the end-to-end job (0: the config's)")
     ap.add_argument("--tuned", type=int, default=1, help="use the autotuned launch shapes when recorded")
+    ap.add_argument("--members", type=int, default=64, help="C4 ensemble size")
     ap.add_argument("--tables", default="auto", choices=["auto", "streamed", "records"],
                     help="binary32 element-table layout")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
@@ -443,6 +533,8 @@ def main():
     world, rank, local = dist_setup(args)
     if args.impl == "reference":
         line = bench_reference(args, world, rank)
+    elif args.config == "C4":
+        line = bench_ensemble(args, world, rank, local)
     else:
         from eqdyna_gb300 import build
         if not os.path.exists(build.GPU_LIB):

@@ -183,7 +183,8 @@ def gpu_lib():
         lib.eqd_ensemble_create.argtypes = [C.POINTER(C.c_void_p), C.c_int32, C.POINTER(C.c_void_p)]
         lib.eqd_ensemble_step.argtypes = [C.c_void_p, C.c_int32]
         lib.eqd_ensemble_destroy.argtypes = [C.c_void_p]
-        for name in ("eqd_ensemble_create", "eqd_ensemble_step", "eqd_ensemble_destroy"):
+        lib.eqd_ensemble_time.argtypes = [C.c_void_p, d_p]
+        for name in ("eqd_ensemble_create", "eqd_ensemble_step", "eqd_ensemble_destroy", "eqd_ensemble_time"):
             getattr(lib, name).restype = C.c_int
         lib.eqd_gpu_newton_counts.argtypes = [C.c_void_p, C.POINTER(C.c_int64)]
         lib.eqd_gpu_newton_counts.restype = C.c_int
@@ -200,7 +201,8 @@ GPU_SYMBOLS = ["eqd_gpu_init", "eqd_gpu_step", "eqd_gpu_fetch", "eqd_gpu_fetch_f
                "eqd_gpu_finalize", "eqd_gpu_status_string", "eqd_gpu_stats", "eqd_gpu_time",
                "eqd_gpu_profile", "eqd_gpu_kernel_time", "eqd_gpu_newton_counts", "eqd_gpu_table_info",
                "eqd_gpu_fetch_fric_rows", "eqd_host_alloc", "eqd_host_free",
-               "eqd_ensemble_create", "eqd_ensemble_step", "eqd_ensemble_destroy", "eqd_gpu_init_times",
+               "eqd_ensemble_create", "eqd_ensemble_step", "eqd_ensemble_destroy", "eqd_ensemble_time",
+               "eqd_gpu_init_times",
                "eqd_gpu_newton_log", "eqd_gpu_newton_records", "eqd_gpu_mlp_train", "eqd_gpu_mlp_get",
                "eqd_gpu_mlp_set", "eqd_gpu_mlp_enable", "eqd_gpu_newton_replay", "eqd_mlp_gradient",
                "eqd_gpu_fp64_fma_peak"]

@@ -14,6 +14,9 @@ writes, see eqdyna_gb300.case), seeded with 20261203 + config id.
       241 x 121 fault node pairs, sigma_n -100 MPa, tau0 60 MPa, smooth 25 MPa overstress
       nucleation of radius 3 km at (0, -7.5 km) (TPV104 form), dt 0.004 s,
       4000 steps.
+  C4  64 members of the C0 box, each at a seeded dx from {200, 250, 300, 400} m with its own dt,
+      von Karman initial shear stress (correlation 1-4 km, Hurst 0.8, 5-15 %), seeded
+      hypocentre; advanced as one ensemble, 1500 steps.
   C3  30-degree dipping reverse fault reaching the surface, degenerated wedge elements along
       the fault, slip law, depth-dependent sigma_n (16.2 MPa/km, capped at 120 MPa),
       tau0/sigma_n 0.55 with a 2 km circular patch at 0.75.
@@ -155,9 +158,62 @@ def config_c1(path, scale=1.0, nsteps=4000, npml=None):
     return path
 
 
+def von_karman_field(rng, nz, nx, h, corr, hurst):
+    """Zero-mean, unit-variance 2-D random field with the von Karman spectrum
+    P(k) ~ (1 + (k a)^2)^-(H + 1) (correlation length a, Hurst exponent H) on an nz x nx grid of
+    spacing h: seeded white noise filtered in the Fourier domain (periodic)."""
+    noise = rng.standard_normal((nz, nx))
+    kz = 2.0 * np.pi * np.fft.fftfreq(nz, d=h)
+    kx = 2.0 * np.pi * np.fft.fftfreq(nx, d=h)
+    k2 = kz[:, None] ** 2 + kx[None, :] ** 2
+    amp = (1.0 + k2 * corr * corr) ** (-(hurst + 1.0) / 2.0)
+    f = np.real(np.fft.ifft2(np.fft.fft2(noise) * amp))
+    f -= f.mean()
+    sd = f.std()
+    return f / sd if sd > 0 else f
+
+
+C4_DX = (200.0, 250.0, 300.0, 400.0)
+
+
+def config_c4(path, member, nsteps=1500):
+    """Member `member` (0..63) of the C4 ensemble: the C0 box and slip-weakening fault at a seeded
+    dx from {200, 250, 300, 400} m (dt = 0.008 s * dx / 200 m), initial shear stress
+    60 MPa * (1 + s f) with f a seeded von Karman field (correlation length 1-4 km, Hurst 0.8,
+    s = 5-15 %), and a 3 x 3 km nucleation patch at 72 MPa around a seeded hypocentre."""
+    rng = np.random.default_rng(SEED0 + 4 + 1000 * member)
+    dx = float(C4_DX[int(rng.integers(0, len(C4_DX)))])
+    p = _base_params()
+    p.update(dx=dx, dy=dx, dz=dx, dt=0.008 * dx / 200.0, friclaw=1, tpv=0, C_nuclea=0)
+    p["term"] = nsteps * p["dt"]
+    corr = float(rng.uniform(1.0e3, 4.0e3))
+    sd = float(rng.uniform(0.05, 0.15))
+    hx = float(rng.uniform(-8.0e3, 8.0e3))
+    hz = float(rng.uniform(-10.0e3, -3.0e3))
+    fx, fz = _fault_grid(p)
+    field = von_karman_field(rng, len(fz), len(fx), dx, corr, 0.8)
+    ofv = np.zeros((24, len(fz), len(fx)))
+    F = _NC_INDEX
+    for ix, x in enumerate(fx):
+        for iz, z in enumerate(fz):
+            edge = abs(abs(x) - p["fxmax"]) < 0.01 or abs(z - p["fzmin"]) < 0.01
+            ofv[F[1], iz, ix] = 1000.0 if edge else 0.70
+            ofv[F[2], iz, ix] = 0.50
+            ofv[F[3], iz, ix] = 0.30
+            ofv[F[7], iz, ix] = -100.0e6
+            patch = abs(x - hx) <= 1.5e3 + 1e-6 and abs(z - hz) <= 1.5e3 + 1e-6
+            ofv[F[8], iz, ix] = 72.0e6 if patch else 60.0e6 * (1.0 + sd * field[iz, ix])
+    st_on, st_off = _stations(rng, p, n_on=4, n_off=4)
+    write_case_dir(path, p, [[6000.0, 3464.0, 2670.0]], st_on, st_off, ofv,
+                   gpu_switches={"nPML": 6, "C_hg": 1, "kapa_hg": 0.1})
+    return path
+
+
 CONFIGS = {"C0": config_c0, "C1": config_c1}
 
 WORKLOADS = {
     "C0": "slip-weakening half-space, dx 200 m, 1,469,664 elements (6-layer PML)",
+    "C4": "ensemble of 64 slip-weakening scenarios, dx from {200, 250, 300, 400} m, von Karman initial "
+          "shear stress, seeded hypocentres, one launch per kernel per step",
     "C1": "rate-and-state aging law, dx 100 m, 20,216,000 elements (40-layer PML), learned Newton guess",
 }

@@ -1343,6 +1343,8 @@ struct eqd_ensemble {
   void *nf = nullptr;  // node / fault argument tables
   void *eb = nullptr;  // element argument tables
   cudaGraphExec_t graph = nullptr;
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  double last_ms = 0.0;
 };
 
 namespace {
@@ -1375,7 +1377,9 @@ int eqd_ensemble_create(eqd_context *const *members, int32_t n, eqd_ensemble **o
   E->device = members[0]->c.device;
   cudaSetDevice(E->device);
   int rc = EQD_OK;
-  if (cudaStreamCreateWithFlags(&E->stream, cudaStreamNonBlocking) != cudaSuccess) rc = EQD_ERR_CUDA;
+  if (cudaStreamCreateWithFlags(&E->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&E->ev[0]) != cudaSuccess || cudaEventCreate(&E->ev[1]) != cudaSuccess)
+    rc = EQD_ERR_CUDA;
   if (!rc) {
     for (auto *X : E->members) cudaStreamSynchronize(X->c.stream);
     rc = ensemble_refresh(*E);
@@ -1398,10 +1402,17 @@ int eqd_ensemble_step(eqd_ensemble *E, int32_t nsteps) {
   int done = 0;
   bool first = false;
   for (auto *c : E->ctx) first |= c->f_is_acc != 0;
+  double first_ms = 0.0;
+  EQD_CUDA_OK(cudaEventRecord(E->ev[0], E->stream));
   if (first) {  // members fresh from init consume their stored acceleration in this step
     RC(ensemble_launch_step(*E));
+    EQD_CUDA_OK(cudaEventRecord(E->ev[1], E->stream));
     for (auto *c : E->ctx) c->f_is_acc = 0;
     RC(ensemble_refresh(*E));
+    float ms = 0.f;
+    EQD_CUDA_OK(cudaEventElapsedTime(&ms, E->ev[0], E->ev[1]));
+    first_ms = ms;
+    EQD_CUDA_OK(cudaEventRecord(E->ev[0], E->stream));
     ++done;
   }
   if (nsteps - done >= kGraphSteps) {
@@ -1426,7 +1437,13 @@ int eqd_ensemble_step(eqd_ensemble *E, int32_t nsteps) {
     }
   }
   for (; done < nsteps; ++done) RC(ensemble_launch_step(*E));
+  EQD_CUDA_OK(cudaEventRecord(E->ev[1], E->stream));
   EQD_CUDA_OK(cudaStreamSynchronize(E->stream));
+  {
+    float ms = 0.f;
+    EQD_CUDA_OK(cudaEventElapsedTime(&ms, E->ev[0], E->ev[1]));
+    E->last_ms = first_ms + ms;
+  }
   EQD_CUDA_OK(cudaGetLastError());
   int status = EQD_OK;
   for (auto *X : E->members) {
@@ -1447,10 +1464,19 @@ int eqd_ensemble_destroy(eqd_ensemble *E) {
   cudaSetDevice(E->device);
   if (E->stream) cudaStreamSynchronize(E->stream);
   if (E->graph) cudaGraphExecDestroy(E->graph);
+  for (auto &e : E->ev)
+    if (e) cudaEventDestroy(e);
   node_fault_batch_free(E->nf);
   elem_batch_free(E->eb);
   if (E->stream) cudaStreamDestroy(E->stream);
   delete E;
+  return EQD_OK;
+}
+
+int eqd_ensemble_time(eqd_ensemble *E, double *ms) {
+  if (!E) return EQD_ERR_STATE;
+  if (!ms) return EQD_ERR_INPUT;
+  *ms = E->last_ms;
   return EQD_OK;
 }
 

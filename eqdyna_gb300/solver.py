@@ -227,6 +227,15 @@ class Ensemble:
         for s in self.solvers:
             s.nt += int(nsteps)
 
+    @property
+    def last_step_ms(self):
+        """Device time (CUDA events on the ensemble's stream) of the last step() call."""
+        ms = C.c_double()
+        rc = self.lib.eqd_ensemble_time(self._h, C.byref(ms))
+        if rc != 0:
+            raise N.EqdError(rc, "eqd_ensemble_time")
+        return ms.value
+
     def close(self):
         if self._h:
             self.lib.eqd_ensemble_destroy(self._h)

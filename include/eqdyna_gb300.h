@@ -255,6 +255,8 @@ int eqd_ensemble_create(eqd_context *const *members, int32_t n, eqd_ensemble **e
 /* Advances every member by nsteps steps (each from its own current step). */
 int eqd_ensemble_step(eqd_ensemble *ens, int32_t nsteps);
 int eqd_ensemble_destroy(eqd_ensemble *ens);
+/* Device time (ms, CUDA events on the ensemble's stream) of the last eqd_ensemble_step call. */
+int eqd_ensemble_time(eqd_ensemble *ens, double *ms);
 
 /* Wall time (ms) of the phases of eqd_gpu_init: 0 nodes (and the device context), 1 element
  * grouping and ordering, 2 element tables, 3 binary32 tiles, 4 binary32 tables and element uploads,
