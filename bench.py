@@ -64,7 +64,7 @@ NODE_BYTES = {"fp64": (152, 536), "fp32": (148, 340)}
 # (profiles/elem_f32_uniform_C1-dx200.md), scaled to a launch by its element count.
 NCU_TRAFFIC_PER_UNIT = {("elem_interior", "records", 1): (105.420032e6 + 10.960384e6) / 1125000,
                         ("elem_pml", "records", 1): (256.453376e6 + 106.076672e6) / 1402000}
-JOB_STEPS = {"C0": 1000, "C1": 4000}
+JOB_STEPS = {"C0": 1000, "C1": 4000, "C3": 5000}
 # the result a host program reads after every step: fric rows 71-76 (slip s/d/n, slip rate s/d,
 # peak slip rate) of every fault pair
 RESULT_ROWS = [71, 72, 73, 74, 75, 76]
@@ -102,6 +102,10 @@ class ClockSampler:
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            t0 = time.perf_counter()
+            while not self.lines and time.perf_counter() - t0 < 5.0 and self.proc.poll() is None:
+                time.sleep(0.01)  # the sampler is running before the timed region starts
+        self.first = max(len(self.lines) - 1, 0)  # the last sample before the region, then all inside
         return self
 
     def _read(self):
@@ -119,7 +123,7 @@ class ClockSampler:
     def summary(self):
         sm, mx, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in self.lines:
+        for line in self.lines[getattr(self, "first", 0):]:
             parts = [p.strip() for p in line.split(",")]
             if len(parts) < 9:
                 continue
@@ -511,7 +515,7 @@ def bench_ensemble(args, world, rank, local):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=40)
+    ap.add_argument("--steps", type=int, default=400)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--config", default="C1")
     ap.add_argument("--scale", type=float, default=1.0)

@@ -158,6 +158,70 @@ def config_c1(path, scale=1.0, nsteps=4000, npml=None):
     return path
 
 
+def config_c3(path, scale=1.0, nsteps=5000, L=0.2, patch_ratio=0.75, patch_radius=2.0e3):
+    """30-degree dipping reverse fault reaching the free surface (down-dip width 20 km, 40 km along
+    strike), as the reference builds dipping faults (case_input/test.tpv36): cells of dx along
+    strike, dx cos(dip) and dx sin(dip) across it, hexahedra along the fault degenerated into wedge
+    pairs (C_degen = dip), dt = 0.5 dz / vp (scripts/defaultParameters.py mod4dip).  Slip law with
+    strong rate weakening (TPV104 form: a = 0.01 rising by 0.01 and Vw from 0.1 by 0.9 outside a
+    smooth core, b 0.014, V0 1e-6, f0 0.6, fw 0.2; L 0.2 m, half TPV104's, because with 0.4 m the
+    2 km patch stays below the nucleation size and creeps for tens of seconds), initial slip rate
+    1e-12 m/s and the state at steady state for the background stress; sigma_n = 16.2 MPa/km x depth
+    capped at 120 MPa (floored at 1 MPa at the surface); dip shear 0.55 sigma_n moving the hanging
+    wall (y+) up, 0.75 sigma_n in a 2 km circle at 10 km down dip.  The initial creep rate points
+    along the initial shear (bGPU.txt vini_along_shear): the reference always starts it along
+    strike, which leaves a dip-loaded rate-and-state fault out of equilibrium at the first step."""
+    dip = 30.0
+    sd, cd = math.sin(math.radians(dip)), math.cos(math.radians(dip))
+    width, length = 20.0e3, 40.0e3
+    p = _base_params()
+    dx = 100.0 * scale
+    dy, dz = dx * cd, dx * sd
+    p.update(dx=dx, dy=dy, dz=dz, dt=0.5 * dz / 6000.0, friclaw=4, tpv=0, C_nuclea=0, dip=dip, C_degen=dip,
+             insertFaultType=0,
+             xmin=-length / 2 - 3.0e3, xmax=length / 2 + 3.0e3, ymin=-4.0e3, ymax=width * cd + 4.0e3,
+             zmin=-width * sd - 4.0e3, zmax=0.0,
+             fxmin=-length / 2, fxmax=length / 2, fymin=0.0, fymax=width * cd, fzmin=-width * sd, fzmax=0.0,
+             nuni_y_minus=5, nuni_y_plus=int(round(width / dx)) + 5, enlarging_ratio=1.025,
+             xsource=0.0, ysource=10.0e3 * cd, zsource=-10.0e3 * sd)
+    p["term"] = nsteps * p["dt"]
+    rng = np.random.default_rng(SEED0 + 3)
+    nfx = int(round((p["fxmax"] - p["fxmin"]) / dx)) + 1
+    nfz = int(round((p["fzmax"] - p["fzmin"]) / dz)) + 1
+    fx = np.linspace(p["fxmin"], p["fxmax"], nfx)
+    fz = np.linspace(p["fzmin"], p["fzmax"], nfz)
+    ofv = np.zeros((24, nfz, nfx))
+    F = _NC_INDEX
+    a0, da, b, V0, f0, fw, vw0, dvw, Vini = 0.01, 0.01, 0.014, 1e-6, 0.6, 0.2, 0.1, 0.9, 1e-12
+    for ix, x in enumerate(fx):
+        for iz, z in enumerate(fz):
+            downdip = abs(z) / sd
+            core = _smooth_box(x, length / 2 - 3.0e3, 3.0e3) * _smooth_box(downdip - width / 2, width / 2 - 3.0e3, 3.0e3)
+            a = a0 + da * (1.0 - core)
+            sigma = max(min(16.2e6 * abs(z) / 1e3, 120.0e6), 1.0e6)
+            ratio = patch_ratio if math.hypot(x, downdip - 10.0e3) <= patch_radius else 0.55
+            tau = ratio * sigma
+            ofv[F[9], iz, ix] = a
+            ofv[F[10], iz, ix] = b
+            ofv[F[11], iz, ix] = L
+            ofv[F[12], iz, ix] = V0
+            ofv[F[13], iz, ix] = f0
+            ofv[F[14], iz, ix] = fw
+            ofv[F[15], iz, ix] = vw0 + dvw * (1.0 - core)
+            ofv[F[46], iz, ix] = Vini
+            ofv[F[7], iz, ix] = -sigma
+            ofv[F[8], iz, ix] = 0.0
+            ofv[F[49], iz, ix] = tau
+            # background steady state (0.55), so the overstressed patch accelerates and nucleates
+            ofv[F[20], iz, ix] = a * math.log(2.0 * V0 / Vini * math.sinh(0.55 / a))
+            ofv[F[1], iz, ix], ofv[F[2], iz, ix], ofv[F[3], iz, ix] = 0.7, 0.5, 0.3
+    st_on = np.array([[0.0, 0.0], [0.0, -2.5], [0.0, -5.0], [10.0, -5.0], [-10.0, -2.5]])
+    st_off = np.array([[0.0, -2.0, 0.0], [0.0, 2.0, 0.0], [10.0, 8.0, 0.0], [0.0, 16.0, 0.0]])
+    write_case_dir(path, p, [[6000.0, 3464.0, 2670.0]], st_on, st_off, ofv,
+                   gpu_switches={"nPML": 6, "C_hg": 1, "kapa_hg": 0.1, "vini_along_shear": 1})
+    return path
+
+
 def von_karman_field(rng, nz, nx, h, corr, hurst):
     """Zero-mean, unit-variance 2-D random field with the von Karman spectrum
     P(k) ~ (1 + (k a)^2)^-(H + 1) (correlation length a, Hurst exponent H) on an nz x nx grid of
@@ -209,10 +273,12 @@ def config_c4(path, member, nsteps=1500):
     return path
 
 
-CONFIGS = {"C0": config_c0, "C1": config_c1}
+CONFIGS = {"C0": config_c0, "C1": config_c1, "C3": config_c3}
 
 WORKLOADS = {
     "C0": "slip-weakening half-space, dx 200 m, 1,469,664 elements (6-layer PML)",
+    "C3": "30-degree dipping reverse fault to the surface, wedge elements along the fault, slip law, "
+          "dx 100 m along strike and dip, learned Newton guess",
     "C4": "ensemble of 64 slip-weakening scenarios, dx from {200, 250, 300, 400} m, von Karman initial "
           "shear stress, seeded hypocentres, one launch per kernel per step",
     "C1": "rate-and-state aging law, dx 100 m, 20,216,000 elements (40-layer PML), learned Newton guess",

@@ -131,6 +131,10 @@ struct Inputs {
   // compile-time constants of the reference made runtime switches (bGPU.txt)
   int nPML = 6, C_Q = 0, C_hg = 1;
   double R = 0.01, kapa_hg = 0.1, rdampm = 0.0;
+  // extension with no reference counterpart: the initial creep rate along the initial shear
+  // traction instead of along strike (src/netcdf_io.f90:98-100 always uses strike), for
+  // rate-and-state faults loaded along dip
+  int vini_along_shear = 0;
 };
 
 double mat_in(const Inputs &in, int i, int j) {  // material(i,j), 1-based
@@ -295,6 +299,7 @@ void read_inputs(const std::string &dir, Inputs &in) {
       else if (key == "C_Q") in.C_Q = static_cast<int>(val);
       else if (key == "C_hg") in.C_hg = static_cast<int>(val);
       else if (key == "kapa_hg") in.kapa_hg = val;
+      else if (key == "vini_along_shear") in.vini_along_shear = static_cast<int>(val);
       else if (key == "rdampm") in.rdampm = val;
       else fail("unknown key '" + key + "' in bGPU.txt");
     }
@@ -833,6 +838,11 @@ void on_fault_fields(Case &c) {
     f[26] = f[46];
     f[27] = 0.0;
     f[5] = V(ii, jj, 22);  f[4] = V(ii, jj, 23);  f[49] = V(ii, jj, 24);
+    const double tau = std::hypot(f[8], f[49]);
+    if (in.vini_along_shear && tau > 0.0) {
+      f[26] = f[46] * f[8] / tau;
+      f[27] = f[46] * f[49] / tau;
+    }
     f[23] = std::fabs(f[7]);
   }
 }

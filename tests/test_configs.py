@@ -1,0 +1,45 @@
+"""Configuration generators (CPU): the C3 dipping thrust builds wedge pairs along the fault and starts
+in equilibrium away from its nucleation patch; C4 members differ in mesh size and stress field."""
+import tempfile
+
+import numpy as np
+
+from conftest import nthreads
+
+
+def test_c3_wedges_and_initial_equilibrium():
+    from eqdyna_gb300.case import Case
+    from eqdyna_gb300.configs import config_c3
+    from oracle import Oracle
+    case = Case.from_dir(config_c3(tempfile.mkdtemp(prefix="eqd_c3_"), scale=8.0, nsteps=10))
+    et = case.arrays["elemTypeArr"]
+    assert (et == 11).sum() > 0 and (et == 11).sum() == (et == 12).sum() and (et == 13).sum() > 0
+    assert case.scalars.friclaw == 4
+    fr = case.fric()
+    # creep along the initial shear (dip direction): fric(26) = 0, fric(27) = Vini
+    assert np.all(fr[:, 25] == 0.0) and np.all(fr[:, 26] == fr[:, 45])
+    xyz = case.fault_coords()
+    sd = np.sin(np.radians(30.0))
+    downdip = np.abs(xyz[:, 2]) / sd
+    patch = np.hypot(xyz[:, 0], downdip - 10.0e3) <= 2.0e3 + 1.0
+    assert patch.sum() >= 1
+    o = Oracle(case, nthreads())
+    o.step(3)
+    fr = case.fric()
+    rate = np.hypot(fr[:, 73], fr[:, 74])
+    far = np.hypot(xyz[:, 0], downdip - 10.0e3) > 6.0e3
+    assert rate[patch].max() > 0.01          # the overstressed patch slips at once
+    assert rate[far].max() < 1e-9            # the background stays at its creep rate
+    o.close()
+
+
+def test_c4_members_differ():
+    from eqdyna_gb300.case import Case
+    from eqdyna_gb300.configs import config_c4
+    dx, tau = set(), []
+    for m in range(6):
+        c = Case.from_dir(config_c4(tempfile.mkdtemp(prefix="eqd_c4_"), m, nsteps=4))
+        dx.add(round(c.scalars.dx))
+        tau.append(float(c.fric()[:, 7].std()))
+    assert len(dx) >= 2
+    assert all(t > 0.0 for t in tau) and len({round(t, 3) for t in tau}) == len(tau)
