@@ -10,6 +10,7 @@
 #include <vector>
 
 #include "eqd_device.cuh"
+#include "fpconv.cuh"
 #include "mlp_common.cuh"
 #include "rsf_newton.cuh"
 
@@ -109,13 +110,16 @@ struct NodeArgs32 {
   const double *Fsplit;
   const int *split_slot;
   int f_is_acc;  // used by the batched launch (the single launch selects a template instead)
+  int damp;      // rdampk != 0: the element kernels read u + rdampk v instead of u
 };
 
 // Node update of the binary32 form.  The force sums arrive in binary32 (Kahan-compensated per
 // tile); acceleration, its increment a*dt and the PML split-field velocities are binary32, while
 // velocity and displacement of every node stay binary64 (increments are small against the state,
-// which is accumulated over 10^3 - 10^4 steps).  About 6 binary64 operations per component.
-// Split (fault) nodes are updated entirely in binary64.
+// which is accumulated over 10^3 - 10^4 steps).  Two binary64 operations per component (v += dv,
+// u += v dt; a third for u + rdampk v when stiffness damping is on); the conversions between the
+// formats run on the integer pipe (fpconv.cuh).  Split (fault) nodes are updated entirely in
+// binary64.
 template <bool F_IS_ACC>
 __device__ __forceinline__ void node_update32_body(const NodeArgs32 &a, int i) {
   double *__restrict__ vel = a.vel;
@@ -156,18 +160,22 @@ __device__ __forceinline__ void node_update32_body(const NodeArgs32 &a, int i) {
       dl32[c * nnode + i] = (float)fma(rdampk, v[c], u);
     }
   } else if (i < n_int) {
+    float v32[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       const float f = F[c * nnode + i];
       const float dv = F_IS_ACC ? f * dt : f * im * dt;
-      v[c] = vel[c * nnode + i] + (double)dv;
-      vel[c * nnode + i] = v[c];
-      const double u = fma(v[c], dtd, disp[c * nnode + i]);
+      const double vn = vel[c * nnode + i] + widen_f32(dv);
+      vel[c * nnode + i] = vn;
+      const double u = fma(vn, dtd, disp[c * nnode + i]);
       disp[c * nnode + i] = u;
       F[c * nnode + i] = 0.f;
-      vel32[c * nnode + i] = (float)v[c];
-      dl32[c * nnode + i] = (float)fma(rdampk, v[c], u);
+      v32[c] = narrow_f64(vn);
+      vel32[c * nnode + i] = v32[c];
+      dl32[c * nnode + i] = narrow_f64(a.damp ? fma(rdampk, vn, u) : u);
     }
+    if (isnan(v32[0]) || isnan(v32[1]) || isnan(v32[2])) atomicOr(d_err, 1);
+    return;
   } else {
     const int p = i - n_int;
     if (im == 0.f) {
@@ -194,20 +202,24 @@ __device__ __forceinline__ void node_update32_body(const NodeArgs32 &a, int i) {
         vs[j / 3] += nv;
         F9[j * npml + p] = 0.f;
       }
+      float v32[3];
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
         const float f = F[c * nnode + i];
         const float dv = F_IS_ACC ? f * dt : f * im * dt;
-        const double nh = vh[c * npml + p] + (double)dv;
+        const double nh = vh[c * npml + p] + widen_f32(dv);
         vh[c * npml + p] = nh;
-        v[c] = (double)vs[c] + nh;
-        vel[c * nnode + i] = v[c];
-        const double u = fma(v[c], dtd, disp[c * nnode + i]);
+        const double vn = widen_f32(vs[c]) + nh;
+        vel[c * nnode + i] = vn;
+        const double u = fma(vn, dtd, disp[c * nnode + i]);
         disp[c * nnode + i] = u;
         F[c * nnode + i] = 0.f;
-        vel32[c * nnode + i] = (float)v[c];
-        dl32[c * nnode + i] = (float)fma(rdampk, v[c], u);
+        v32[c] = narrow_f64(vn);
+        vel32[c * nnode + i] = v32[c];
+        dl32[c * nnode + i] = narrow_f64(a.damp ? fma(rdampk, vn, u) : u);
       }
+      if (isnan(v32[0]) || isnan(v32[1]) || isnan(v32[2])) atomicOr(d_err, 1);
+      return;
     }
   }
   if (isnan(v[0]) || isnan(v[1]) || isnan(v[2])) atomicOr(d_err, 1);
@@ -635,6 +647,7 @@ NodeArgs32 node_args32(const Context &c) {
   a.split_slot = c.split_slot;
   a.nsplit = 2 * c.npair;
   a.f_is_acc = c.f_is_acc;
+  a.damp = c.sc.rdampk != 0.0;
   return a;
 }
 
@@ -789,4 +802,68 @@ int launch_fault(Context &c, cudaStream_t s) {
   return cudaGetLastError() == cudaSuccess ? EQD_OK : EQD_ERR_CUDA;
 }
 
+namespace {
+
+__device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
+  z += 0x9e3779b97f4a7c15ull;
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+
+// widen_f32 / narrow_f64 against the hardware conversions: every binary32 pattern class (random
+// bits), and binary64 values with exponents 880..1160 (around and inside the binary32 normal range)
+// whose dropped 29 fraction bits are random, exactly half (ties), just below and just above half,
+// or whose kept 23 bits are all ones (carry into the exponent).
+__global__ void fpconv_check_kernel(long long n, unsigned long long seed, unsigned long long *bad) {
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+    const unsigned long long h = mix64(seed ^ (unsigned long long)k);
+    const float f = __uint_as_float((unsigned)h);
+    const double w1 = widen_f32(f), w2 = (double)f;
+    const bool okw = __double_as_longlong(w1) == __double_as_longlong(w2) || (isnan(w1) && isnan(w2));
+    const unsigned long long g = mix64(h);
+    const unsigned long long e = 880ull + g % 281ull;
+    unsigned long long frac = mix64(g) & ((1ull << 52) - 1ull);
+    const unsigned long long low = 0x1fffffffull;
+    switch (k & 7) {
+      case 1: frac = (frac & ~low) | 0x10000000ull; break;
+      case 2: frac = (frac & ~low) | 0x0fffffffull; break;
+      case 3: frac = (frac & ~low) | 0x10000001ull; break;
+      case 4: frac |= ~low & ((1ull << 52) - 1ull); break;
+      case 5: frac = (frac | (~low & ((1ull << 52) - 1ull)) & ~low) | 0x10000000ull; break;
+      default: break;
+    }
+    const double d = __longlong_as_double((long long)(((h >> 63) << 63) | (e << 52) | frac));
+    const float n1 = narrow_f64(d), n2 = (float)d;
+    const bool okn = __float_as_uint(n1) == __float_as_uint(n2) || (isnan(n1) && isnan(n2));
+    if (!okw) atomicAdd(bad, 1ull);
+    if (!okn) atomicAdd(bad + 1, 1ull);
+  }
+}
+
+}  // namespace
+
 }  // namespace eqd
+
+extern "C" int eqd_gpu_check_conversions(int32_t device, int64_t n, uint64_t seed, int64_t mismatches[2]) {
+  using namespace eqd;
+  if (n <= 0 || !mismatches) return EQD_ERR_INPUT;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return EQD_ERR_NO_DEVICE;
+  }
+  EQD_CUDA_OK(cudaSetDevice(device));
+  unsigned long long *bad = nullptr;
+  if (cudaMalloc(reinterpret_cast<void **>(&bad), 2 * sizeof(unsigned long long)) != cudaSuccess) return EQD_ERR_OOM;
+  int rc = EQD_OK;
+  unsigned long long hb[2] = {0, 0};
+  cudaMemset(bad, 0, sizeof(hb));
+  fpconv_check_kernel<<<4 * 152, 256>>>(n, seed, bad);
+  if (cudaDeviceSynchronize() != cudaSuccess || cudaMemcpy(hb, bad, sizeof(hb), cudaMemcpyDeviceToHost) != cudaSuccess)
+    rc = EQD_ERR_CUDA;
+  cudaFree(bad);
+  mismatches[0] = (int64_t)hb[0];
+  mismatches[1] = (int64_t)hb[1];
+  return rc;
+}

@@ -241,6 +241,11 @@ int eqd_gpu_newton_replay(eqd_context *ctx, int32_t learned, int32_t fast, int64
 int eqd_mlp_gradient(int32_t device, const float *params, const float *x, const float *t, int32_t n,
                      float *loss, float *grad);
 
+/* Self-check of the integer-pipe conversions between binary32 and binary64 that the binary32 node
+ * update uses, against the hardware conversions, over n seeded operands in each direction:
+ * mismatches = {binary32 -> binary64, binary64 -> binary32} (both 0 on a correct build). */
+int eqd_gpu_check_conversions(int32_t device, int64_t n, uint64_t seed, int64_t mismatches[2]);
+
 /* ---- ensembles -----------------------------------------------------------------------------
  * No counterpart in the reference (one scenario per process there).  Several contexts created by
  * eqd_gpu_init on the same device — rupture scenarios of any mesh size and time step — advance

@@ -116,3 +116,13 @@ def test_fp32_form_within_budget_on_c1_shape():
             rel = np.linalg.norm(y - x) / np.linalg.norm(x)
             print(" ", key, rel)
             assert rel <= 1e-3
+
+
+def test_integer_pipe_conversions_match_hardware():
+    """The binary32 node update converts between binary32 and binary64 with integer operations;
+    they must give the hardware conversions' bits (16.8 M operands each way, ties and carries)."""
+    import ctypes as C
+    from eqdyna_gb300 import _native as N
+    mm = (C.c_int64 * 2)()
+    assert N.gpu_lib().eqd_gpu_check_conversions(0, 1 << 24, 20261204, mm) == 0
+    assert list(mm) == [0, 0]
