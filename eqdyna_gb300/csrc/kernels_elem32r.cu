@@ -28,6 +28,10 @@ using namespace e32;
 
 namespace {
 
+// Shared-memory rows of a tile (kTile floats each).  Every per-element row is read and written
+// only by the thread of its element (column), and each thread reads its copied rows before it
+// writes its per-corner forces, so the force rows overlay the copied rows: a CTA needs
+// max(copied, 24) rows instead of copied + 24 (more CTAs per SM).
 template <bool BODY, bool PLASTIC, int HG>
 struct RecInterior {
   static constexpr int REM = TabCommon<HG>::STR;         // record: 8 corner masses after mu
@@ -35,20 +39,22 @@ struct RecInterior {
   static constexpr int POR = 6;                          // 1 pore pressure
   static constexpr int RID = POR + (PLASTIC ? 1 : 0);    // record index (u32)
   static constexpr int N = RID + 1;                      // rows copied
-  static constexpr int FS = N;                           // 24 rows of per-corner forces
-  static constexpr int NS = N + 24;
+  static constexpr int FS = 0;                           // 24 rows of per-corner forces (overlay)
+  static constexpr int NS = 24;
 };
 template <bool BODY, bool S0, int HG>
 struct RecPml {
   static constexpr int REM = TabCommon<HG>::STR;
-  static constexpr int STR = 0;                          // 15 split-field stress
-  static constexpr int ST0 = 15;                         // 6 initial stress
-  static constexpr int RID = ST0 + (S0 ? 6 : 0);
-  static constexpr int ABID = RID + 1;                   // 2 rows of PML axis indices (u32)
-  static constexpr int N = ABID + 2;
-  static constexpr int FS = N;
+  static constexpr int RID = 0;                          // record index (u32): read again by the
+                                                         // node gather, so never overlaid
+  static constexpr int ABID = 1;                         // 2 rows of PML axis indices (u32)
+  static constexpr int STR = 3;                          // 15 split-field stress
+  static constexpr int ST0 = 18;                         // 6 initial stress
+  static constexpr int N = ST0 + (S0 ? 6 : 0);
   static constexpr int ES = STR;                         // 6 split-stress sums over the stress rows
-  static constexpr int NS = N + 24;
+  static constexpr int FS = ES + 6;                      // 24 rows of per-corner forces (overlay)
+  static constexpr int NS = FS + 24;
+  static_assert(NS >= N, "copied rows fit");
 };
 
 template <class L>
