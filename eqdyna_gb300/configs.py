@@ -90,7 +90,9 @@ def _fault_grid(p):
     return fx, fz
 
 
-def config_c0(path, scale=1.0, nsteps=1000):
+def config_c0(path, scale=1.0, nsteps=1000, **switches):
+    """C0 slip-weakening half-space; `switches` are extra bGPU.txt switches (e.g. C_Q=1 for the
+    coarse-grained Q model)."""
     p = _base_params()
     dx = 200.0 * scale
     p.update(dx=dx, dy=dx, dz=dx, dt=0.008 * scale, friclaw=1, tpv=0, C_nuclea=0)
@@ -110,7 +112,7 @@ def config_c0(path, scale=1.0, nsteps=1000):
             ofv[F[8], iz, ix] = 72.0e6 if patch else 60.0e6
     st_on, st_off = _stations(rng, p)
     write_case_dir(path, p, [[6000.0, 3464.0, 2670.0]], st_on, st_off, ofv,
-                   gpu_switches={"nPML": 6, "C_hg": 1, "kapa_hg": 0.1})
+                   gpu_switches=dict({"nPML": 6, "C_hg": 1, "kapa_hg": 0.1}, **switches))
     return path
 
 

@@ -111,20 +111,48 @@ struct TabCommon {
   static constexpr int STR = MU + 1;
 };
 
-// Gathers the binary32 node data of tile t; returns the tile's node count.
+// Shared memory of a tile after its per-element rows: the incidence list, the slot table, the
+// staged node data, the tile's incidence pointers and (optionally) its node ids.
+struct TileSmem {
+  unsigned short *sinc;     // [8 * kTile] incidences (corner * kTile + element), node-major
+  unsigned short *slot_of;  // [8 * kTile] local node of (corner, element)
+  float *sv, *sd;           // [3][Mmax] binary32 velocity and u + rdampk v of the tile's nodes
+  unsigned short *sincp;    // [Mmax + 1] first incidence of each tile node
+  int *sids;                // [Mmax] global node ids, or null (read again from the tile list)
+};
+__device__ __forceinline__ TileSmem tile_smem(float *rows_end, int Mmax, bool ids) {
+  TileSmem t;
+  t.sinc = reinterpret_cast<unsigned short *>(rows_end);
+  t.slot_of = t.sinc + 8 * kTile;
+  t.sv = reinterpret_cast<float *>(t.slot_of + 8 * kTile);
+  t.sd = t.sv + 3 * Mmax;
+  t.sids = ids ? reinterpret_cast<int *>(t.sd + 3 * Mmax) : nullptr;
+  t.sincp = reinterpret_cast<unsigned short *>(t.sd + 3 * Mmax + (ids ? Mmax : 0));
+  return t;
+}
+inline size_t tile_smem_bytes(int Mmax, bool ids) {
+  return 2 * (8 * kTile * 2) + 6 * (size_t)Mmax * 4 + (ids ? 4 * (size_t)Mmax : 0) + (((size_t)Mmax + 2) & ~(size_t)1) * 2;
+}
+
+// Stages tile t: the binary32 node data, the incidence pointers and (optionally) the node ids
+// into shared memory, all loads of a node issued together; returns the tile's node count.
 __device__ __forceinline__ int stage_nodes(const ElemGroup<float> &g, int t, const float *__restrict__ vel32,
-                                           const float *__restrict__ dl32, int nnode, int Mmax, float *sv,
-                                           float *sd, int &nb) {
+                                           const float *__restrict__ dl32, int nnode, int Mmax,
+                                           const TileSmem &ts, int &nb) {
   nb = g.tile_node_ptr[t];
   const int M = g.tile_node_ptr[t + 1] - nb;
+  const unsigned short *__restrict__ incp = g.tile_incp + g.tile_incp_off[t];
   for (int j = threadIdx.x; j < M; j += blockDim.x) {
     const int n = g.tile_nodes[nb + j];
+    ts.sincp[j] = incp[j];
+    if (ts.sids) ts.sids[j] = n;
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-      sv[c * Mmax + j] = vel32[c * nnode + n];
-      sd[c * Mmax + j] = dl32[c * nnode + n];
+      ts.sv[c * Mmax + j] = vel32[c * nnode + n];
+      ts.sd[c * Mmax + j] = dl32[c * nnode + n];
     }
   }
+  if (threadIdx.x == 0) ts.sincp[M] = incp[M];
   return M;
 }
 
@@ -141,13 +169,17 @@ __device__ __forceinline__ void build_slots(const unsigned short *incp, int M, c
 // Interior element (types 1, 11-13): stress update, optional Drucker-Prager return, stiffness +
 // Rayleigh + hourglass + body forces per corner into fs[(c * 8 + a) * kTile + tid].  fs may
 // overlay the hourglass-vector rows of S: each corner's rows are written only after they were read.
-template <bool BODY, bool PLASTIC, int HG, class Src>
+// QM: coarse-grained Q (src/calcElemKU.f90:77-132): the stress follows from the strain of the
+// displacement u = (u + rdampk v) - rdampk v and the 6 memory variables (stress rows 6-11), with
+// the element's constants S.q(0..4) = exp(-dt / tau_k), mu c_s, (lambda + 2 mu) c_v, 8 w_kp, 8 w_ks.
+template <bool BODY, bool PLASTIC, int HG, bool QM, class Src>
 __device__ __forceinline__ void interior_element(const Src &S, const float *sv, const float *sd, int Mmax,
                                                  const unsigned short *slot_of, int tid,
                                                  const ElemConst32 &k, double *pstrain_e,
                                                  float *stress_e, size_t ld, float *fs) {
   using C = TabCommon<HG>;
   float sr[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  float sn[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};  // strain (QM only)
   float ph[4][3];
 #pragma unroll
   for (int m = 0; m < 4; ++m) ph[m][0] = ph[m][1] = ph[m][2] = 0.f;
@@ -163,6 +195,16 @@ __device__ __forceinline__ void interior_element(const Src &S, const float *sv, 
     sr[3] = fmaf(by, vz, fmaf(bz, vy, sr[3]));
     sr[4] = fmaf(bx, vz, fmaf(bz, vx, sr[4]));
     sr[5] = fmaf(bx, vy, fmaf(by, vx, sr[5]));
+    if constexpr (QM) {
+      const float ux = fmaf(-k.rdampk, vx, sd[sl[a]]), uy = fmaf(-k.rdampk, vy, sd[Mmax + sl[a]]);
+      const float uz = fmaf(-k.rdampk, vz, sd[2 * Mmax + sl[a]]);
+      sn[0] = fmaf(bx, ux, sn[0]);
+      sn[1] = fmaf(by, uy, sn[1]);
+      sn[2] = fmaf(bz, uz, sn[2]);
+      sn[3] = fmaf(by, uz, fmaf(bz, uy, sn[3]));
+      sn[4] = fmaf(bx, uz, fmaf(bz, ux, sn[4]));
+      sn[5] = fmaf(bx, uy, fmaf(by, ux, sn[5]));
+    }
     if (HG == 1) {
       const float lx = sd[sl[a]], ly = sd[Mmax + sl[a]], lz = sd[2 * Mmax + sl[a]];
 #pragma unroll
@@ -186,8 +228,23 @@ __device__ __forceinline__ void interior_element(const Src &S, const float *sv, 
   const float srate[6] = {cd * sr[0] + lam * sr[1] + lam * sr[2], lam * sr[0] + cd * sr[1] + lam * sr[2],
                           lam * sr[0] + lam * sr[1] + cd * sr[2], mu * sr[3], mu * sr[4], mu * sr[5]};
   float s[6];
+  if constexpr (!QM) {
 #pragma unroll
-  for (int i = 0; i < 6; ++i) s[i] = fmaf(srate[i], k.dt, S.str(i));
+    for (int i = 0; i < 6; ++i) s[i] = fmaf(srate[i], k.dt, S.str(i));
+  } else {
+    const float ex = S.q(0), miuu = S.q(1), Mu = S.q(2), wkp = S.q(3), wks = S.q(4);
+    const float vols = sn[0] + sn[1] + sn[2];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+      const float a1 = S.str(6 + i);
+      const float drive = (i < 3) ? 2.f * miuu * sn[i] * wks + (Mu * wkp - 2.f * miuu * wks) * vols
+                                  : miuu * sn[i] * wks;
+      const float an = ex * a1 + (1.f - ex) * drive;
+      stress_e[(6 + i) * ld] = an;
+      s[i] = (i < 3) ? 2.f * miuu * sn[i] + (Mu - 2.f * miuu) * vols - 0.5f * (an + a1)
+                     : miuu * sn[i] - 0.5f * (an + a1);
+    }
+  }
   if (PLASTIC) {
     const float strmea = (s[0] + s[1] + s[2]) / 3.0f;
     const float dev[6] = {s[0] - strmea, s[1] - strmea, s[2] - strmea, s[3], s[4], s[5]};
@@ -266,7 +323,8 @@ __device__ __forceinline__ void interior_element(const Src &S, const float *sv, 
 // order, one binary32 L2 reduction per component.
 __device__ __forceinline__ void interior_gather(const ElemGroup<float> &g, int M, int nb,
                                                 const unsigned short *incp, const unsigned short *sinc,
-                                                const float *fs, float *__restrict__ F, int nnode) {
+                                                const float *fs, float *__restrict__ F, int nnode,
+                                                const int *sids) {
   for (int j = threadIdx.x; j < M; j += blockDim.x) {
     float hi[3] = {0.f, 0.f, 0.f}, lo[3] = {0.f, 0.f, 0.f};
     const int q1 = incp[j + 1];
@@ -276,7 +334,7 @@ __device__ __forceinline__ void interior_gather(const ElemGroup<float> &g, int M
 #pragma unroll
       for (int c = 0; c < 3; ++c) kahan_add(hi[c], lo[c], fs[(c * 8 + a) * kTile + el]);
     }
-    const int n = g.tile_nodes[nb + j];
+    const int n = sids ? sids[j] : g.tile_nodes[nb + j];
 #pragma unroll
     for (int c = 0; c < 3; ++c) atomicAdd(F + (size_t)c * nnode + n, hi[c] - lo[c]);
   }
@@ -400,7 +458,7 @@ template <class WOf>
 __device__ __forceinline__ void pml_gather(const ElemGroup<float> &g, int M, int nb, const unsigned short *incp,
                                            const unsigned short *sinc, const float *es, const float *cfh,
                                            const WOf &w_of, float *__restrict__ F, float *__restrict__ F9,
-                                           int nnode, int n_int, int npml) {
+                                           int nnode, int n_int, int npml, const int *sids) {
   for (int j = threadIdx.x; j < M; j += blockDim.x) {
     float hi[12], lo[12];
 #pragma unroll
@@ -420,7 +478,7 @@ __device__ __forceinline__ void pml_gather(const ElemGroup<float> &g, int M, int
 #pragma unroll
       for (int c = 0; c < 3; ++c) kahan_add(hi[9 + c], lo[9 + c], cfh[(c * 8 + a) * kTile + el]);
     }
-    const int n = g.tile_nodes[nb + j];
+    const int n = sids ? sids[j] : g.tile_nodes[nb + j];
     if (n >= n_int) {
       const int slot = n - n_int;
 #pragma unroll

@@ -22,7 +22,7 @@ namespace eqd {
 ElemConst make_elem_const(const Context &c);
 int tile_size_interior();
 int tile_size_pml();
-int record_length(int hg, bool body);
+int record_length(int hg, bool body, bool q);
 }  // namespace eqd
 
 using namespace eqd;
@@ -316,6 +316,8 @@ int validate(const eqd_scalars *s, const eqd_host_arrays *a) {
   if (s->C_hg != 1 && s->C_hg != 2) return EQD_ERR_UNSUPPORTED;
   if (a->ntotft != 1 && a->ntotft != 0) return EQD_ERR_UNSUPPORTED;
   if (s->friclaw < 1 || s->friclaw > 5) return EQD_ERR_INPUT;
+  // the reference stops on Q with plasticity (src/warning.f90:6-9, stop 1001)
+  if (s->C_Q == 1 && s->C_elastic == 0) return EQD_ERR_UNSUPPORTED;
   return EQD_OK;
 }
 
@@ -461,7 +463,9 @@ int build_device_state(eqd_context &X, const eqd_scalars &s, const eqd_host_arra
   }
   const bool body = (s.rdampm != 0.0) || (s.C_elastic == 0);
   if (c.fp32) {
-    if (s.C_Q == 1) return EQD_ERR_UNSUPPORTED;  // Q memory variables: binary64 form only
+    // Q memory variables in the binary32 form: record-indexed tables only (the Q constants are
+    // part of an element's record)
+    if (s.C_Q == 1 && c.opt.table_layout == EQD_TABLES_STREAMED) return EQD_ERR_UNSUPPORTED;
     const int ts = c.opt.tile_shape > 0 ? c.opt.tile_shape : (4 | 8 << 8 | 4 << 16);
     const int bx = ts & 255, by = (ts >> 8) & 255, bz = (ts >> 16) & 255;
     brick_order(a, X.gi_orig, bx, bz, by);
@@ -571,12 +575,13 @@ int build_device_state(eqd_context &X, const eqd_scalars &s, const eqd_host_arra
       // record-indexed layout: one record per distinct binary32 (geometry, material) combination
       const int layout = c.opt.table_layout;
       bool use_rec = layout != EQD_TABLES_STREAMED;
-      RecordDict dict(record_length(s.C_hg, body));
+      const bool qm = grp == 0 && s.C_Q == 1;
+      RecordDict dict(record_length(s.C_hg, body, qm));
       std::vector<unsigned> rid, abid;
       std::vector<float> abt;
       if (use_rec) {
         // per-thread dictionaries over contiguous chunks, merged in chunk order
-        const long cap = layout == EQD_TABLES_RECORDS ? (long)m : std::min<long>(kAutoMaxRecords, m / 2 + 1);
+        const long cap = (layout == EQD_TABLES_RECORDS || qm) ? (long)m : std::min<long>(kAutoMaxRecords, m / 2 + 1);
         rid.assign(ld, 0u);
         const int T = std::max(1, omp_get_max_threads());
         std::vector<RecordDict> local(T, RecordDict(dict.len()));
@@ -599,6 +604,8 @@ int build_device_state(eqd_context &X, const eqd_scalars &s, const eqd_host_arra
             r[q++] = (float)mu[i];
             if (body)
               for (int k = 0; k < 8; ++k) r[q++] = (float)em[k * um + i];
+            if (qm)
+              for (int k = 0; k < 5; ++k) r[q++] = (float)qc[k * um + i];
             const long id = local[t].find_or_add(r.data(), cap);
             if (id < 0) {
               overflow[t] = 1;
@@ -662,7 +669,7 @@ int build_device_state(eqd_context &X, const eqd_scalars &s, const eqd_host_arra
             std::copy(pairs[k].begin(), pairs[k].end(), abt.begin() + 2 * (size_t)k * h.ab_stride);
         }
       }
-      if (!use_rec && layout == EQD_TABLES_RECORDS) return EQD_ERR_UNSUPPORTED;
+      if (!use_rec && (layout == EQD_TABLES_RECORDS || qm)) return EQD_ERR_UNSUPPORTED;
       if (use_rec) {
         h.nrec = (int)dict.size();
         h.rec_len = dict.len();
@@ -800,10 +807,10 @@ int build_device_state(eqd_context &X, const eqd_scalars &s, const eqd_host_arra
   // ---- step bookkeeping ----
   RC(dalloc(c, c.d_nt, 1));
   RC(dalloc(c, c.d_err, 1));
-  RC(dalloc(c, c.d_stats, 4));
+  RC(dalloc(c, c.d_stats, 5));
   EQD_CUDA_OK(cudaMemset(c.d_nt, 0, sizeof(int)));
   EQD_CUDA_OK(cudaMemset(c.d_err, 0, sizeof(int)));
-  EQD_CUDA_OK(cudaMemset(c.d_stats, 0, 4 * sizeof(unsigned long long)));
+  EQD_CUDA_OK(cudaMemset(c.d_stats, 0, 5 * sizeof(unsigned long long)));
   c.nt = 0;
   c.time = s.time0;
   X.times.assign(1, s.time0);
@@ -1322,15 +1329,15 @@ int eqd_gpu_mlp_enable(eqd_context *X, int32_t on) {
   return EQD_OK;
 }
 
-int eqd_gpu_newton_replay(eqd_context *X, int32_t learned, int32_t fast, int64_t counts[4], double *v_host) {
+int eqd_gpu_newton_replay(eqd_context *X, int32_t learned, int32_t fast, int64_t counts[5], double *v_host) {
   if (!X) return EQD_ERR_STATE;
   if (!counts) return EQD_ERR_INPUT;
   Context &c = X->c;
   cudaSetDevice(c.device);
   EQD_CUDA_OK(cudaStreamSynchronize(c.stream));
-  long long cc[4] = {0, 0, 0, 0};
+  long long cc[5] = {0, 0, 0, 0, 0};
   RC(newton_replay(c, learned, fast, cc, v_host));
-  for (int k = 0; k < 4; ++k) counts[k] = cc[k];
+  for (int k = 0; k < 5; ++k) counts[k] = cc[k];
   return EQD_OK;
 }
 
@@ -1480,15 +1487,15 @@ int eqd_ensemble_time(eqd_ensemble *E, double *ms) {
   return EQD_OK;
 }
 
-int eqd_gpu_newton_counts(eqd_context *X, int64_t out[4]) {
+int eqd_gpu_newton_counts(eqd_context *X, int64_t out[5]) {
   if (!X) return EQD_ERR_STATE;
   if (!out) return EQD_ERR_INPUT;
   Context &c = X->c;
-  unsigned long long st[4] = {0, 0, 0, 0};
+  unsigned long long st[5] = {0, 0, 0, 0, 0};
   cudaSetDevice(c.device);
   EQD_CUDA_OK(cudaStreamSynchronize(c.stream));
   EQD_CUDA_OK(cudaMemcpy(st, c.d_stats, sizeof(st), cudaMemcpyDeviceToHost));
-  for (int k = 0; k < 4; ++k) out[k] = (int64_t)st[k];
+  for (int k = 0; k < 5; ++k) out[k] = (int64_t)st[k];
   return EQD_OK;
 }
 

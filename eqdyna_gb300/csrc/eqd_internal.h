@@ -126,8 +126,9 @@ struct Context {
   int *d_nt = nullptr;          // current step index on the device
   double *d_times = nullptr;    // [nstep + 2] timeElapsed after nt steps
   int *d_err = nullptr;         // error word: 1 = NaN velocity, 2 = bounded wait gave up
-  unsigned long long *d_stats = nullptr;  // [4]: Newton iterations (as counted by the reference),
-                                          // ivmax hits, iterations executed, learned guesses used
+  unsigned long long *d_stats = nullptr;  // [5]: Newton iterations (as counted by the reference),
+                                          // ivmax hits, iterations executed, learned guesses used,
+                                          // learned solves repeated from the plain guess
   int nt = 0;                   // steps completed (host mirror)
   double time = 0.0;
   int f_is_acc = 0;             // first node update consumes acceleration (from init state)
@@ -170,6 +171,6 @@ int newton_records(Context &c, double *host, long long cap, long long *count);
 int mlp_train(Context &c, const eqd_mlp_train_options &o, float *epoch_loss, float *holdout_loss);
 int mlp_get(Context &c, float *params, float *norm);
 int mlp_set(Context &c, const float *params, const float *norm);
-int newton_replay(Context &c, int learned, int fast, long long counts[4], double *v_host);
+int newton_replay(Context &c, int learned, int fast, long long counts[5], double *v_host);
 
 }  // namespace eqd

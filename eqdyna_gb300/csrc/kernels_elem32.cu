@@ -30,6 +30,7 @@ struct SlabInterior : TabCommon<HG> {
   // per-(corner, element) forces [3][8]: over the hourglass vectors when there are some
   static constexpr int FS = HG == 1 ? B::PHI : N;
   static constexpr int NS = HG == 1 ? N : N + 24;        // rows in shared memory
+  static constexpr bool IDS = false;  // node ids staged in shared memory
 };
 template <bool BODY, bool S0, int HG>
 struct SlabPml : TabCommon<HG> {
@@ -41,6 +42,7 @@ struct SlabPml : TabCommon<HG> {
   static constexpr int FS = HG == 1 ? B::PHI : N;
   static constexpr int ES = B::STR;                      // 6 split-stress sums over the stress rows
   static constexpr int NS = HG == 1 ? N : N + 24;
+  static constexpr bool IDS = true;  // node ids staged in shared memory
 };
 
 // Table source reading column `col` of the staged slab.
@@ -82,10 +84,9 @@ __global__ void __launch_bounds__(kTile)
   __shared__ __align__(8) unsigned long long bar;
   const int Mmax = g.max_tile_nodes;
   float *tab = reinterpret_cast<float *>(smem);
-  unsigned short *sinc = reinterpret_cast<unsigned short *>(tab + L::NS * kTile);  // [8 * kTile]
-  unsigned short *slot_of = sinc + 8 * kTile;                                     // [8 * kTile]
-  float *sv = reinterpret_cast<float *>(slot_of + 8 * kTile);
-  float *sd = sv + 3 * Mmax;
+  const TileSmem ts = tile_smem(tab + L::NS * kTile, Mmax, false);
+  unsigned short *sinc = ts.sinc, *slot_of = ts.slot_of;
+  float *sv = ts.sv, *sd = ts.sd;
   const int tid = threadIdx.x;
   const int e0 = blockIdx.x * kTile;
   const int ld = g.ld;
@@ -100,18 +101,19 @@ __global__ void __launch_bounds__(kTile)
   }
   __syncthreads();  // barrier initialised before anyone polls it
   int nb;
-  const int M = stage_nodes(g, blockIdx.x, vel32, dl32, nnode, Mmax, sv, sd, nb);
+  const int M = stage_nodes(g, blockIdx.x, vel32, dl32, nnode, Mmax, ts, nb);
   const bool ok = mbar_wait_bounded(&bar, err);
-  const unsigned short *incp = g.tile_incp + g.tile_incp_off[blockIdx.x];
-  if (ok) build_slots(incp, M, sinc, slot_of);
+  const unsigned short *incp = ts.sincp;
   if (__syncthreads_or(!ok)) return;  // the whole CTA skips the tile if any thread gave up
+  build_slots(incp, M, sinc, slot_of);  // reads the staged pointers of other threads
+  __syncthreads();
   const int e = e0 + tid;
   float *fs = tab + L::FS * kTile;
   if (e < g.ne)
-    interior_element<BODY, PLASTIC, HG>(SlabSrc<L>{tab, tid}, sv, sd, Mmax, slot_of, tid, k,
+    interior_element<BODY, PLASTIC, HG, false>(SlabSrc<L>{tab, tid}, sv, sd, Mmax, slot_of, tid, k,
                                         PLASTIC ? g.pstrain + e : nullptr, g.stress + e, (size_t)ld, fs);
   __syncthreads();
-  interior_gather(g, M, nb, incp, sinc, fs, F, nnode);
+  interior_gather(g, M, nb, incp, sinc, fs, F, nnode, ts.sids);
 }
 
 template <bool BODY, bool S0, int HG>
@@ -124,10 +126,9 @@ __global__ void __launch_bounds__(kTile)
   __shared__ __align__(8) unsigned long long bar;
   const int Mmax = g.max_tile_nodes;
   float *tab = reinterpret_cast<float *>(smem);
-  unsigned short *sinc = reinterpret_cast<unsigned short *>(tab + L::NS * kTile);
-  unsigned short *slot_of = sinc + 8 * kTile;
-  float *sv = reinterpret_cast<float *>(slot_of + 8 * kTile);
-  float *sd = sv + 3 * Mmax;
+  const TileSmem ts = tile_smem(tab + L::NS * kTile, Mmax, true);
+  unsigned short *sinc = ts.sinc, *slot_of = ts.slot_of;
+  float *sv = ts.sv, *sd = ts.sd;
   const int tid = threadIdx.x;
   const int e0 = blockIdx.x * kTile;
   const int ld = g.ld;
@@ -143,11 +144,12 @@ __global__ void __launch_bounds__(kTile)
   }
   __syncthreads();
   int nb;
-  const int M = stage_nodes(g, blockIdx.x, vel32, dl32, nnode, Mmax, sv, sd, nb);
+  const int M = stage_nodes(g, blockIdx.x, vel32, dl32, nnode, Mmax, ts, nb);
   const bool ok = mbar_wait_bounded(&bar, err);
-  const unsigned short *incp = g.tile_incp + g.tile_incp_off[blockIdx.x];
-  if (ok) build_slots(incp, M, sinc, slot_of);
-  if (__syncthreads_or(!ok)) return;
+  const unsigned short *incp = ts.sincp;
+  if (__syncthreads_or(!ok)) return;  // the whole CTA skips the tile if any thread gave up
+  build_slots(incp, M, sinc, slot_of);  // reads the staged pointers of other threads
+  __syncthreads();
   const int e = e0 + tid;
   float *cfh = tab + L::FS * kTile;
   float *es = tab + L::ES * kTile;
@@ -156,12 +158,12 @@ __global__ void __launch_bounds__(kTile)
                               es, cfh);
   __syncthreads();
   auto src_of = [&](int el) { return SlabSrc<L>{tab, el}; };
-  pml_gather(g, M, nb, incp, sinc, es, cfh, w_from_src<HG>(src_of), F, F9, nnode, n_int, npml);
+  pml_gather(g, M, nb, incp, sinc, es, cfh, w_from_src<HG>(src_of), F, F9, nnode, n_int, npml, ts.sids);
 }
 
 template <class L>
 size_t slab_smem(int Mmax) {
-  return (size_t)L::NS * kTile * 4 + 2 * (8 * kTile * 2) + 6 * (size_t)Mmax * 4;
+  return (size_t)L::NS * kTile * 4 + tile_smem_bytes(Mmax, L::IDS);
 }
 
 template <bool BODY, bool PLASTIC, int HG>

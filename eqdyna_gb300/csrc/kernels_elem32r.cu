@@ -32,15 +32,18 @@ namespace {
 // only by the thread of its element (column), and each thread reads its copied rows before it
 // writes its per-corner forces, so the force rows overlay the copied rows: a CTA needs
 // max(copied, 24) rows instead of copied + 24 (more CTAs per SM).
-template <bool BODY, bool PLASTIC, int HG>
+template <bool BODY, bool PLASTIC, int HG, bool QM = false>
 struct RecInterior {
   static constexpr int REM = TabCommon<HG>::STR;         // record: 8 corner masses after mu
+  static constexpr int QC = REM + (BODY ? 8 : 0);        // record: 5 Q constants (QM)
   static constexpr int STR = 0;                          // shared-memory rows: 6 stress
-  static constexpr int POR = 6;                          // 1 pore pressure
+                                                         // (+ 6 Q memory variables)
+  static constexpr int POR = QM ? 12 : 6;                // 1 pore pressure
   static constexpr int RID = POR + (PLASTIC ? 1 : 0);    // record index (u32)
   static constexpr int N = RID + 1;                      // rows copied
   static constexpr int FS = 0;                           // 24 rows of per-corner forces (overlay)
   static constexpr int NS = 24;
+  static constexpr bool IDS = false;                     // node ids re-read by the gather
 };
 template <bool BODY, bool S0, int HG>
 struct RecPml {
@@ -54,6 +57,7 @@ struct RecPml {
   static constexpr int ES = STR;                         // 6 split-stress sums over the stress rows
   static constexpr int FS = ES + 6;                      // 24 rows of per-corner forces (overlay)
   static constexpr int NS = FS + 24;
+  static constexpr bool IDS = true;                      // node ids staged in shared memory
   static_assert(NS >= N, "copied rows fit");
 };
 
@@ -67,6 +71,7 @@ struct RecSrc {
   unsigned ab01, ab2; // axis indices: x | y << 16, z
   __device__ float g(int row) const { return __ldg(rec + row); }
   __device__ float em(int a) const { return __ldg(rec + L::REM + a); }
+  __device__ float q(int i) const { return __ldg(rec + L::QC + i); }
   __device__ float str(int i) const { return tab[(L::STR + i) * kTile + col]; }
   __device__ float por() const { return tab[L::POR * kTile + col]; }
   __device__ float st0(int i) const { return tab[(L::ST0 + i) * kTile + col]; }
@@ -88,6 +93,7 @@ struct UniSrc {
   unsigned ab01, ab2;
   __device__ float g(int row) const { return r.v[row]; }
   __device__ float em(int a) const { return r.v[L::REM + a]; }
+  __device__ float q(int i) const { return r.v[L::QC + i]; }
   __device__ float str(int i) const { return tab[(L::STR + i) * kTile + col]; }
   __device__ float por() const { return tab[L::POR * kTile + col]; }
   __device__ float st0(int i) const { return tab[(L::ST0 + i) * kTile + col]; }
@@ -114,18 +120,17 @@ struct ElemArgs32 {
   RecordParam rp;
 };
 
-template <bool BODY, bool PLASTIC, int HG, bool UNI>
+template <bool BODY, bool PLASTIC, int HG, bool UNI, bool QM>
 __device__ __forceinline__ void interior_rec_body(const ElemArgs32 &a, int tile) {
-  using L = RecInterior<BODY, PLASTIC, HG>;
+  using L = RecInterior<BODY, PLASTIC, HG, QM>;
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) unsigned long long bar;
   const ElemGroup<float> &g = a.g;
   const int Mmax = g.max_tile_nodes;
   float *tab = reinterpret_cast<float *>(smem);
-  unsigned short *sinc = reinterpret_cast<unsigned short *>(tab + L::NS * kTile);
-  unsigned short *slot_of = sinc + 8 * kTile;
-  float *sv = reinterpret_cast<float *>(slot_of + 8 * kTile);
-  float *sd = sv + 3 * Mmax;
+  const TileSmem ts = tile_smem(tab + L::NS * kTile, Mmax, L::IDS);
+  unsigned short *sinc = ts.sinc, *slot_of = ts.slot_of;
+  float *sv = ts.sv, *sd = ts.sd;
   const int tid = threadIdx.x;
   const int e0 = tile * kTile;
   const int ld = g.ld;
@@ -133,31 +138,32 @@ __device__ __forceinline__ void interior_rec_body(const ElemArgs32 &a, int tile)
     mbar_init(&bar, 1);
     mbar_expect_tx(&bar, (unsigned)(L::N * kTile * 4 + 8 * kTile * 2));
     bulk_g2s(sinc, g.tile_inc + (size_t)tile * kTile * 8, 8 * kTile * 2, &bar);
-    copy_rows(tab, L::STR, g.stress, 6, ld, e0, &bar);
+    copy_rows(tab, L::STR, g.stress, QM ? 12 : 6, ld, e0, &bar);
     if (PLASTIC) copy_rows(tab, L::POR, g.porep, 1, ld, e0, &bar);
     copy_rows(tab, L::RID, g.rec_id, 1, ld, e0, &bar);
   }
   __syncthreads();
   int nb;
-  const int M = stage_nodes(g, tile, a.vel32, a.dl32, a.nnode, Mmax, sv, sd, nb);
+  const int M = stage_nodes(g, tile, a.vel32, a.dl32, a.nnode, Mmax, ts, nb);
   const bool ok = mbar_wait_bounded(&bar, a.err);
-  const unsigned short *incp = g.tile_incp + g.tile_incp_off[tile];
-  if (ok) build_slots(incp, M, sinc, slot_of);
-  if (__syncthreads_or(!ok)) return;
+  const unsigned short *incp = ts.sincp;
+  if (__syncthreads_or(!ok)) return;  // the whole CTA skips the tile if any thread gave up
+  build_slots(incp, M, sinc, slot_of);  // reads the staged pointers of other threads
+  __syncthreads();
   const int e = e0 + tid;
   float *fs = tab + L::FS * kTile;
   if (e < g.ne) {
     double *ps = PLASTIC ? g.pstrain + e : nullptr;
     if (UNI) {
       const UniSrc<L> S{a.rp, tab, tid, nullptr, 0, 0u, 0u};
-      interior_element<BODY, PLASTIC, HG>(S, sv, sd, Mmax, slot_of, tid, a.k, ps, g.stress + e, (size_t)ld, fs);
+      interior_element<BODY, PLASTIC, HG, QM>(S, sv, sd, Mmax, slot_of, tid, a.k, ps, g.stress + e, (size_t)ld, fs);
     } else {
       const RecSrc<L> S{g.rec + (size_t)row_u32(tab, L::RID, tid) * g.rec_len, tab, tid, nullptr, 0, 0u, 0u};
-      interior_element<BODY, PLASTIC, HG>(S, sv, sd, Mmax, slot_of, tid, a.k, ps, g.stress + e, (size_t)ld, fs);
+      interior_element<BODY, PLASTIC, HG, QM>(S, sv, sd, Mmax, slot_of, tid, a.k, ps, g.stress + e, (size_t)ld, fs);
     }
   }
   __syncthreads();
-  interior_gather(g, M, nb, incp, sinc, fs, a.F, a.nnode);
+  interior_gather(g, M, nb, incp, sinc, fs, a.F, a.nnode, ts.sids);
 }
 
 template <bool BODY, bool S0, int HG, bool UNI>
@@ -170,10 +176,9 @@ __device__ __forceinline__ void pml_rec_body(const ElemArgs32 &a, int tile) {
   const ElemGroup<float> &g = a.g;
   const int Mmax = g.max_tile_nodes;
   float *tab = reinterpret_cast<float *>(smem);
-  unsigned short *sinc = reinterpret_cast<unsigned short *>(tab + L::NS * kTile);
-  unsigned short *slot_of = sinc + 8 * kTile;
-  float *sv = reinterpret_cast<float *>(slot_of + 8 * kTile);
-  float *sd = sv + 3 * Mmax;
+  const TileSmem ts = tile_smem(tab + L::NS * kTile, Mmax, L::IDS);
+  unsigned short *sinc = ts.sinc, *slot_of = ts.slot_of;
+  float *sv = ts.sv, *sd = ts.sd;
   const int tid = threadIdx.x;
   const int e0 = tile * kTile;
   const int ld = g.ld;
@@ -189,11 +194,12 @@ __device__ __forceinline__ void pml_rec_body(const ElemArgs32 &a, int tile) {
   if (UNI && tid < 24) cw[tid] = a.rp.v[C::DET] * a.rp.v[C::SHP + tid];
   __syncthreads();
   int nb;
-  const int M = stage_nodes(g, tile, a.vel32, a.dl32, a.nnode, Mmax, sv, sd, nb);
+  const int M = stage_nodes(g, tile, a.vel32, a.dl32, a.nnode, Mmax, ts, nb);
   const bool ok = mbar_wait_bounded(&bar, a.err);
-  const unsigned short *incp = g.tile_incp + g.tile_incp_off[tile];
-  if (ok) build_slots(incp, M, sinc, slot_of);
-  if (__syncthreads_or(!ok)) return;
+  const unsigned short *incp = ts.sincp;
+  if (__syncthreads_or(!ok)) return;  // the whole CTA skips the tile if any thread gave up
+  build_slots(incp, M, sinc, slot_of);  // reads the staged pointers of other threads
+  __syncthreads();
   const int e = e0 + tid;
   float *cfh = tab + L::FS * kTile;
   float *es = tab + L::ES * kTile;
@@ -217,20 +223,21 @@ __device__ __forceinline__ void pml_rec_body(const ElemArgs32 &a, int tile) {
       wy = cw[3 * c + 1];
       wz = cw[3 * c + 2];
     };
-    pml_gather(g, M, nb, incp, sinc, es, cfh, w_of, a.F, a.F9, a.nnode, a.n_int, a.npml);
+    pml_gather(g, M, nb, incp, sinc, es, cfh, w_of, a.F, a.F9, a.nnode, a.n_int, a.npml, ts.sids);
   } else {
     auto src_of = [&](int el) {
       return RecSrc<L>{rec + (size_t)row_u32(tab, L::RID, el) * rlen, tab, el, nullptr, 0, 0u, 0u};
     };
-    pml_gather(g, M, nb, incp, sinc, es, cfh, w_from_src<HG>(src_of), a.F, a.F9, a.nnode, a.n_int, a.npml);
+    pml_gather(g, M, nb, incp, sinc, es, cfh, w_from_src<HG>(src_of), a.F, a.F9, a.nnode, a.n_int, a.npml,
+               ts.sids);
   }
 }
 
 // One group of one context: arguments in parameter space (record values become constant-bank
 // operands in the UNI variant).
-template <bool BODY, bool PLASTIC, int HG, bool UNI>
+template <bool BODY, bool PLASTIC, int HG, bool UNI, bool QM>
 __global__ void __launch_bounds__(kTile) elem_interior_rec(const __grid_constant__ ElemArgs32 a) {
-  interior_rec_body<BODY, PLASTIC, HG, UNI>(a, blockIdx.x);
+  interior_rec_body<BODY, PLASTIC, HG, UNI, QM>(a, blockIdx.x);
 }
 template <bool BODY, bool S0, int HG, bool UNI>
 __global__ void __launch_bounds__(kTile) elem_pml_rec(const __grid_constant__ ElemArgs32 a) {
@@ -257,13 +264,13 @@ __device__ __forceinline__ int load_member(const ElemArgs32 *__restrict__ args, 
   __syncthreads();
   return blockIdx.x - start[m];
 }
-template <bool BODY, bool PLASTIC, int HG>
+template <bool BODY, bool PLASTIC, int HG, bool QM>
 __global__ void __launch_bounds__(kTile) elem_interior_rec_batched(const ElemArgs32 *__restrict__ args,
                                                                    const int *__restrict__ start, int n) {
   __shared__ __align__(16) ElemArgs32 a;
   const int tile = load_member(args, start, n, a);
-  if (a.g.nrec == 1) interior_rec_body<BODY, PLASTIC, HG, true>(a, tile);
-  else interior_rec_body<BODY, PLASTIC, HG, false>(a, tile);
+  if (a.g.nrec == 1) interior_rec_body<BODY, PLASTIC, HG, true, QM>(a, tile);
+  else interior_rec_body<BODY, PLASTIC, HG, false, QM>(a, tile);
 }
 template <bool BODY, bool S0, int HG>
 __global__ void __launch_bounds__(kTile) elem_pml_rec_batched(const ElemArgs32 *__restrict__ args,
@@ -276,7 +283,7 @@ __global__ void __launch_bounds__(kTile) elem_pml_rec_batched(const ElemArgs32 *
 
 template <class L>
 size_t rec_smem(int Mmax) {
-  return (size_t)L::NS * kTile * 4 + 2 * (8 * kTile * 2) + 6 * (size_t)Mmax * 4;
+  return (size_t)L::NS * kTile * 4 + tile_smem_bytes(Mmax, L::IDS);
 }
 
 ElemArgs32 elem_args(const Context &c, bool interior, const ElemConst32 &k) {
@@ -299,22 +306,23 @@ ElemArgs32 elem_args(const Context &c, bool interior, const ElemConst32 &k) {
 struct Variant {
   bool body, plastic, s0;
   int hg;
+  bool q;  // Q memory variables (elastic only)
 };
 Variant variant_of(const Context &c) {
   return Variant{(c.sc.rdampm != 0.0) || (c.sc.C_elastic == 0), c.sc.C_elastic == 0, c.gp32.stress0 != nullptr,
-                 c.sc.C_hg == 2 ? 2 : 1};
+                 c.sc.C_hg == 2 ? 2 : 1, c.sc.C_Q == 1};
 }
 
-template <bool BODY, bool PLASTIC, int HG>
+template <bool BODY, bool PLASTIC, int HG, bool QM>
 int launch_interior(Context &c, cudaStream_t s, const ElemConst32 &k) {
   const ElemArgs32 a = elem_args(c, true, k);
-  const size_t sm = rec_smem<RecInterior<BODY, PLASTIC, HG>>(a.g.max_tile_nodes);
+  const size_t sm = rec_smem<RecInterior<BODY, PLASTIC, HG, QM>>(a.g.max_tile_nodes);
   if (a.g.nrec == 1) {
-    auto kern = elem_interior_rec<BODY, PLASTIC, HG, true>;
+    auto kern = elem_interior_rec<BODY, PLASTIC, HG, true, QM>;
     if (allow_smem(kern, sm)) return EQD_ERR_CUDA;
     kern<<<a.g.ntiles, kTile, sm, s>>>(a);
   } else {
-    auto kern = elem_interior_rec<BODY, PLASTIC, HG, false>;
+    auto kern = elem_interior_rec<BODY, PLASTIC, HG, false, QM>;
     if (allow_smem(kern, sm)) return EQD_ERR_CUDA;
     kern<<<a.g.ntiles, kTile, sm, s>>>(a);
   }
@@ -341,18 +349,21 @@ template <int HG>
 int launch_hg(Context &c, cudaStream_t s, const ElemConst32 &k, bool interior) {
   const Variant v = variant_of(c);
   if (interior) {
-    if (v.plastic) return v.body ? launch_interior<true, true, HG>(c, s, k) : launch_interior<false, true, HG>(c, s, k);
-    return v.body ? launch_interior<true, false, HG>(c, s, k) : launch_interior<false, false, HG>(c, s, k);
+    if (v.plastic)
+      return v.body ? launch_interior<true, true, HG, false>(c, s, k) : launch_interior<false, true, HG, false>(c, s, k);
+    if (v.q)
+      return v.body ? launch_interior<true, false, HG, true>(c, s, k) : launch_interior<false, false, HG, true>(c, s, k);
+    return v.body ? launch_interior<true, false, HG, false>(c, s, k) : launch_interior<false, false, HG, false>(c, s, k);
   }
   if (v.body) return v.s0 ? launch_pml<true, true, HG>(c, s, k) : launch_pml<true, false, HG>(c, s, k);
   return v.s0 ? launch_pml<false, true, HG>(c, s, k) : launch_pml<false, false, HG>(c, s, k);
 }
 
 // ---- ensembles ----------------------------------------------------------------------------------
-template <bool BODY, bool PLASTIC, int HG>
+template <bool BODY, bool PLASTIC, int HG, bool QM>
 int launch_interior_batched(const ElemArgs32 *args, const int *start, int n, int tiles, int Mmax, cudaStream_t s) {
-  const size_t sm = rec_smem<RecInterior<BODY, PLASTIC, HG>>(Mmax);
-  auto kern = elem_interior_rec_batched<BODY, PLASTIC, HG>;
+  const size_t sm = rec_smem<RecInterior<BODY, PLASTIC, HG, QM>>(Mmax);
+  auto kern = elem_interior_rec_batched<BODY, PLASTIC, HG, QM>;
   if (allow_smem(kern, sm)) return EQD_ERR_CUDA;
   kern<<<tiles, kTile, sm, s>>>(args, start, n);
   return EQD_OK;
@@ -370,10 +381,13 @@ int launch_batched_hg(const Variant &v, bool interior, const ElemArgs32 *args, c
                       int Mmax, cudaStream_t s) {
   if (interior) {
     if (v.plastic)
-      return v.body ? launch_interior_batched<true, true, HG>(args, start, n, tiles, Mmax, s)
-                    : launch_interior_batched<false, true, HG>(args, start, n, tiles, Mmax, s);
-    return v.body ? launch_interior_batched<true, false, HG>(args, start, n, tiles, Mmax, s)
-                  : launch_interior_batched<false, false, HG>(args, start, n, tiles, Mmax, s);
+      return v.body ? launch_interior_batched<true, true, HG, false>(args, start, n, tiles, Mmax, s)
+                    : launch_interior_batched<false, true, HG, false>(args, start, n, tiles, Mmax, s);
+    if (v.q)
+      return v.body ? launch_interior_batched<true, false, HG, true>(args, start, n, tiles, Mmax, s)
+                    : launch_interior_batched<false, false, HG, true>(args, start, n, tiles, Mmax, s);
+    return v.body ? launch_interior_batched<true, false, HG, false>(args, start, n, tiles, Mmax, s)
+                  : launch_interior_batched<false, false, HG, false>(args, start, n, tiles, Mmax, s);
   }
   if (v.body)
     return v.s0 ? launch_pml_batched<true, true, HG>(args, start, n, tiles, Mmax, s)
@@ -393,9 +407,9 @@ struct ElemBatch {
 
 }  // namespace
 
-int record_length(int hg, bool body) {
-  const int n = (hg == 2 ? TabCommon<2>::STR : TabCommon<1>::STR) + (body ? 8 : 0);
-  static_assert(TabCommon<1>::STR + 8 <= kRecMax, "record longer than RecordParam");
+int record_length(int hg, bool body, bool q) {
+  const int n = (hg == 2 ? TabCommon<2>::STR : TabCommon<1>::STR) + (body ? 8 : 0) + (q ? 5 : 0);
+  static_assert(TabCommon<1>::STR + 8 + 5 <= kRecMax, "record longer than RecordParam");
   return (n + 3) / 4 * 4;
 }
 
@@ -411,7 +425,7 @@ int elem_batch_update(void **handle, Context *const *m, int n, const ElemConst *
   const Variant v = variant_of(*m[0]);
   for (int i = 0; i < n; ++i) {
     const Variant w = variant_of(*m[i]);
-    if (!m[i]->fp32 || w.body != v.body || w.plastic != v.plastic || w.s0 != v.s0 || w.hg != v.hg)
+    if (!m[i]->fp32 || w.body != v.body || w.plastic != v.plastic || w.s0 != v.s0 || w.hg != v.hg || w.q != v.q)
       return EQD_ERR_UNSUPPORTED;
     for (int grp = 0; grp < 2; ++grp) {
       const ElemGroup<float> &g = grp == 0 ? m[i]->gi32 : m[i]->gp32;

@@ -438,7 +438,7 @@ __device__ __forceinline__ void fault_body(const FaultArgs &p, int tid,
   }
   tr[3] = sqrt(tr[1] * tr[1] + tr[2] * tr[2]);
 
-  unsigned iters = 0, maxhit = 0, executed = 0, learned = 0;
+  unsigned iters = 0, maxhit = 0, executed = 0, learned = 0, fallback = 0;
   if (p.friclaw <= 2) {
     // solveSWTW (src/faulting.f90:136-188)
     double mu;
@@ -531,7 +531,14 @@ __device__ __forceinline__ void fault_body(const FaultArgs &p, int tid,
       v0 = mlp_guess_warp(*p.mlp, f, vt, full, mlp_xs[threadIdx.x >> 5]);
       learned = 1;
     }
-    const NewtonOut no = rsf_newton<true>(p.friclaw, dt, ns, v0);
+    NewtonOut no = rsf_newton<true>(p.friclaw, dt, ns, v0);
+    if (learned && !newton_settled(no)) {  // the learned guess was outside the Newton's basin
+      const NewtonOut first = no;
+      no = rsf_newton<true>(p.friclaw, dt, ns, vt);
+      no.iters += first.iters;
+      no.executed += first.executed;
+      fallback = 1;
+    }
     const int lstep = nt - p.log_nt0;
     if (p.newton_log && lstep > 0 && lstep % p.log_stride == 0 && lstep / p.log_stride <= p.log_steps) {
       double *rec = p.newton_log + (size_t)kNewtonRecord * ((size_t)(lstep / p.log_stride - 1) * np + i);
@@ -577,6 +584,7 @@ __device__ __forceinline__ void fault_body(const FaultArgs &p, int tid,
     warp_count_add(p.stats + 1, maxhit);
     warp_count_add(p.stats + 2, executed);
     warp_count_add(p.stats + 3, learned);
+    warp_count_add(p.stats + 4, fallback);
   }
   // storeOnFaultStationQuantSCEC
   if (nt >= 1 && nt <= p.nstep) {

@@ -317,12 +317,21 @@ __global__ void __launch_bounds__(128) newton_replay_kernel(const double *__rest
     mlp_features(q[13], q[7], q[9], q[10], q[0], q[1], f);
     v0 = mlp_guess_warp(*m, f, q[13], true, xs[threadIdx.x >> 5]);
   }
-  const NewtonOut o = rsf_newton<FAST>(friclaw, dt, s, v0);
+  NewtonOut o = rsf_newton<FAST>(friclaw, dt, s, v0);
+  unsigned fallback = 0;
+  if (m && !newton_settled(o)) {  // as the fault kernel: repeat from the plain guess
+    const NewtonOut first = o;
+    o = rsf_newton<FAST>(friclaw, dt, s, q[13]);
+    o.iters += first.iters;
+    o.executed += first.executed;
+    fallback = 1;
+  }
   if (live) {
     if (v_out) v_out[i] = o.v;
     warp_count_add(counts + 0, (unsigned)o.iters);
     warp_count_add(counts + 1, (unsigned)o.capped);
     warp_count_add(counts + 2, (unsigned)o.executed);
+    warp_count_add(counts + 3, fallback);
   }
 }
 
@@ -543,7 +552,7 @@ int mlp_train(Context &c, const eqd_mlp_train_options &o, float *epoch_loss, flo
   return rc;
 }
 
-int newton_replay(Context &c, int learned, int fast, long long counts[4], double *v_host) {
+int newton_replay(Context &c, int learned, int fast, long long counts[5], double *v_host) {
   const long long n = newton_log_count(c);
   if (n <= 0) return EQD_ERR_STATE;
   if (learned && !c.mlp) return EQD_ERR_STATE;
@@ -566,6 +575,7 @@ int newton_replay(Context &c, int learned, int fast, long long counts[4], double
     rc = EQD_ERR_CUDA;
   for (int k = 0; k < 3; ++k) counts[k] = (long long)h[k];
   counts[3] = n;
+  counts[4] = (long long)h[3];
   cudaFree(dc);
   if (dv) cudaFree(dv);
   return rc;

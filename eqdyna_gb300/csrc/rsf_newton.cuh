@@ -20,6 +20,7 @@ struct NewtonSolve {
 
 struct NewtonOut {
   double v, state, th, taoc;
+  double step;   // |last Newton step| / |slip rate where it was evaluated|
   int iters;     // as the reference counts them (20 when the cap is reached)
   int capped;    // 1 when the 20 iterations ran out without meeting the tolerance
   int executed;  // iterations actually evaluated
@@ -83,6 +84,7 @@ __device__ __forceinline__ NewtonOut rsf_newton(int friclaw, double dt, const Ne
                                   : 1.0 / (2.0 * p.V0) * exp(s.state0 / p.A);
   double v_eval = v0;                        // FAST: where the law was last evaluated
   double vA = 0.0, thA = 0.0, tcA = 0.0;     // FAST: v_(k-2) and the law evaluated at it
+  double step = 0.0;
   int iv, executed = 0;
   for (iv = 1; iv <= 20; ++iv) {
     ++executed;
@@ -109,6 +111,7 @@ __device__ __forceinline__ NewtonOut rsf_newton(int friclaw, double dt, const Ne
       rsfeq = vt + s.Tc * (taoc_new * 0.5 - s.trial);
       dr = 1.0 + s.Tc * (-dxmudv * fmin(s.tn, 0.0)) * 0.5;
     }
+    step = fabs(rsfeq / dr) / fabs(vt);
     if (fabs(rsfeq / dr) < 1.e-14 * fabs(vt) && fabs(rsfeq) < 1.e-6 * fabs(vt)) break;
     const double vn = vt - rsfeq / dr;
     const double vnew = (vn <= 0.0) ? vt / 2.0 : vn;
@@ -142,10 +145,18 @@ __device__ __forceinline__ NewtonOut rsf_newton(int friclaw, double dt, const Ne
   o.state = stateTmp;
   o.th = thTmp;
   o.taoc = taoc_new;
+  o.step = step;
   o.iters = iv > 20 ? 20 : iv;
   o.capped = iv > 20 ? 1 : 0;
   o.executed = executed;
   return o;
 }
+
+// A solve from the learned initial guess is kept when it settled: it met the exit test, or its
+// last Newton step was below 1e-12 of the slip rate (the iterate had reached round-off, as the
+// plain method's capped solves of creeping pairs do).  A guess outside the Newton's basin ends
+// with the cap reached while the iterate still moves; that solve is repeated from the plain guess
+// and the repeat's result is kept, so a poor guess costs iterations but never changes a result.
+__device__ __forceinline__ bool newton_settled(const NewtonOut &o) { return !o.capped || o.step <= 1.e-12; }
 
 }  // namespace eqd

@@ -90,12 +90,13 @@ class GpuSolver:
 
     def newton_counts(self):
         """Rate-and-state Newton counters since init: iterations as the reference counts them,
-        solves that hit the 20-iteration cap, iterations executed, learned guesses used."""
-        out = (C.c_int64 * 4)()
+        solves that hit the 20-iteration cap, iterations executed, learned guesses used, learned
+        solves repeated from the plain guess."""
+        out = (C.c_int64 * 5)()
         rc = self.lib.eqd_gpu_newton_counts(self._h, out)
         if rc != 0:
             raise N.EqdError(rc, "eqd_gpu_newton_counts")
-        return dict(zip(["iterations", "ivmax_hits", "executed", "learned"], list(out)))
+        return dict(zip(["iterations", "ivmax_hits", "executed", "learned", "fallbacks"], list(out)))
 
     def fetch_fric_rows(self, rows, out):
         """Copy fric rows (1-based) into out[len(rows)][npair] (e.g. a PinnedArray's array)."""
@@ -153,7 +154,7 @@ class GpuSolver:
     def replay(self, learned=False, fast=True, values=False):
         """Re-solve the logged records from the plain or learned guess, with the fault kernel's
         loop (fast) or the reference's loop verbatim: counts (+ slip rates when values=True)."""
-        counts = (C.c_int64 * 4)()
+        counts = (C.c_int64 * 5)()
         v = None
         vp = None
         if values:
@@ -163,7 +164,7 @@ class GpuSolver:
             vp = v.ctypes.data_as(N.c_double_p)
         self._rc(self.lib.eqd_gpu_newton_replay(self._h, int(bool(learned)), int(bool(fast)), counts, vp),
                  "eqd_gpu_newton_replay")
-        out = dict(zip(["iterations", "ivmax_hits", "executed", "records"], list(counts)))
+        out = dict(zip(["iterations", "ivmax_hits", "executed", "records", "fallbacks"], list(counts)))
         return (out, v) if values else out
 
     @staticmethod

@@ -191,10 +191,13 @@ int eqd_gpu_profile(eqd_context *ctx, int32_t enable);
 int eqd_gpu_kernel_time(eqd_context *ctx, int32_t kind, double *ms, int64_t *launches);
 
 /* Rate-and-state Newton counters summed over pairs and steps since init: out[0] iterations as
- * the reference counts them (src/faulting.f90:459-516, at most 20 per solve), out[1] solves that
- * reached 20, out[2] iterations executed (the loop stops early, with identical results, once an
- * iterate repeats), out[3] solves that started from the learned initial guess. */
-int eqd_gpu_newton_counts(eqd_context *ctx, int64_t out[4]);
+ * the reference counts them (src/faulting.f90:459-516, at most 20 per solve; a repeated solve
+ * counts both runs), out[1] solves that reached 20, out[2] iterations executed (the loop stops
+ * early, with identical results, once an iterate repeats), out[3] solves that started from the
+ * learned initial guess, out[4] of those repeated from the plain guess because the run from the
+ * learned guess reached 20 iterations with the iterate still moving (last Newton step above
+ * 1e-12 of the slip rate). */
+int eqd_gpu_newton_counts(eqd_context *ctx, int64_t out[5]);
 
 /* ---- learned initial guess of the rate-and-state Newton solve ------------------------------
  * No counterpart in the reference.  A 6 -> 64 -> 64 -> 1 MLP (BF16 tensor cores, FP32
@@ -231,10 +234,11 @@ int eqd_gpu_mlp_set(eqd_context *ctx, const float *params, const float *norm);
 int eqd_gpu_mlp_enable(eqd_context *ctx, int32_t on);
 /* Re-solves every logged record from the plain (learned = 0) or learned initial guess, with the
  * loop the fault kernel runs (fast = 1: loop-invariant law terms evaluated once, early stop on a
- * repeated iterate, same values bit for bit) or the reference's loop verbatim (fast = 0):
- * counts = {iterations as the reference counts them, solves that reached 20, iterations
- * executed, records}; v_host[records] may be NULL. */
-int eqd_gpu_newton_replay(eqd_context *ctx, int32_t learned, int32_t fast, int64_t counts[4],
+ * repeated iterate, same values bit for bit) or the reference's loop verbatim (fast = 0), and the
+ * fault kernel's repeat from the plain guess: counts = {iterations as the reference counts them,
+ * solves that reached 20, iterations executed, records, repeated solves}; v_host[records] may be
+ * NULL. */
+int eqd_gpu_newton_replay(eqd_context *ctx, int32_t learned, int32_t fast, int64_t counts[5],
                           double *v_host);
 /* Loss sum((y - t)^2) / (2 n) and its gradient for a model and a batch, computed by the training
  * kernel: x[n][6] normalised inputs, t[n] normalised targets (gradient checks). */

@@ -1,10 +1,15 @@
 """C3: 30-degree dipping reverse fault with degenerated wedge elements, slip law, learned guess.
 
-Generated at dx = 400 m (777,632 elements, 5,000 wedge pairs, 5,151 fault pairs) and advanced 200
-steps (3.3 s: the rupture leaves the patch at about 2 s and has broken a fifth of the fault by the
-end): the binary64 form against the oracle (relative 1e-9, Newton iteration counts within 0.1 %),
-the binary32 form with the learned guess (trained on the binary64 run's own solves) within the
-accuracy budget.
+Generated at dx = 400 m (777,632 elements, 5,000 wedge pairs, 5,151 fault pairs).  The overstressed
+patch slips at the first step, creeps, and at about 1.7 s (step 100) the rupture takes off; by
+step 720 (12 s) it has crossed the fault.  The take-off amplifies round-off: the oracle itself,
+with its initial shear perturbed by 1 part in 1e14, differs from the unperturbed oracle by ~3e-13
+at step 90 and by 3e-3 (relative L2 of slip rate) at step 200.  So:
+  * up to step 90 the binary64 form must match the oracle to relative 1e-9, and the binary32 form
+    with the learned guess must stay within the accuracy budget (1 %);
+  * at step 720 the binary64 form must stay within 10x the oracle's own sensitivity to a
+    perturbation of 1e-14, and the binary32 form with the learned guess within the budget on the
+    final slip and the peak slip rate of the completed rupture.
 """
 import tempfile
 
@@ -15,7 +20,12 @@ from conftest import nthreads
 
 pytestmark = pytest.mark.gpu
 
-NSTEPS = 200
+N_EARLY = 90
+N_LATE = 720
+
+
+def _rel(a, b, scale=None):
+    return np.linalg.norm(a - b) / (scale if scale else max(np.linalg.norm(b), 1e-300))
 
 
 @pytest.fixture(scope="module")
@@ -23,53 +33,103 @@ def c3():
     from eqdyna_gb300.case import Case
     from eqdyna_gb300.configs import config_c3
     from oracle import Oracle
-    case = Case.from_dir(config_c3(tempfile.mkdtemp(prefix="eqd_c3_"), scale=4.0, nsteps=NSTEPS))
-    cpu = case.clone()
-    o = Oracle(cpu, nthreads())
-    o.step(NSTEPS)
-    return case, cpu, o
+    case = Case.from_dir(config_c3(tempfile.mkdtemp(prefix="eqd_c3_"), scale=4.0, nsteps=N_LATE))
+    early, late, pert = case.clone(), case.clone(), case.clone()
+    pert.arrays["fric"].reshape(-1, 100)[:, 48] *= 1.0 + 1e-14  # fric(49): initial dip shear
+    o_early = Oracle(early, nthreads())
+    o_early.step(N_EARLY)
+    for c in (late, pert):
+        Oracle(c, nthreads()).step(N_LATE)
+    return case, early, o_early, late, pert
+
+
+def _fields(c):
+    f = c.fric()
+    return {"slip": f[:, 70:72], "slip_rate": f[:, 73:75], "peak_rate": f[:, 75], "vel": c.arrays["velArr"]}
 
 
 def test_c3_mesh_has_wedges(c3):
-    case, _, _ = c3
+    case = c3[0]
     et = case.arrays["elemTypeArr"]
     assert (et == 11).sum() > 0 and (et == 11).sum() == (et == 12).sum() and (et == 13).sum() > 0
     assert case.scalars.friclaw == 4
 
 
-def test_c3_fp64_matches_oracle(c3):
+def test_c3_fp64_matches_oracle_before_take_off(c3):
     from eqdyna_gb300.solver import GpuSolver
     from test_gpu_parity import check_parity
-    case, cpu, o = c3
+    case, early, o_early = c3[:3]
     gpu = case.clone()
     with GpuSolver(gpu, precision="fp64") as s:
-        s.step(NSTEPS)
+        s.step(N_EARLY)
         s.fetch()
         stats = s.stats()
-    print(check_parity(cpu, gpu, case.scalars.dt))
-    ref = o.stats()["newton_iters"]
+    print(check_parity(early, gpu, case.scalars.dt))
+    ref = o_early.stats()["newton_iters"]
     assert abs(stats["newton_iters"] - ref) <= 1e-3 * ref
 
 
-def test_c3_fp32_learned_within_budget(c3):
+def test_c3_fp64_within_oracle_sensitivity_after_take_off(c3):
+    from eqdyna_gb300.solver import GpuSolver
+    case, _, _, late, pert = c3
+    gpu = case.clone()
+    with GpuSolver(gpu, precision="fp64") as s:
+        s.step(N_LATE)
+        s.fetch()
+    rep = _against_sensitivity(late, pert, gpu)
+    print("binary64: gpu vs oracle, oracle perturbed by 1e-14 vs oracle:", rep)
+    assert (late.arrays["fnft"][: case.npair] < 1e4).sum() > 500  # the rupture is under way
+    for k, (ours, own) in rep.items():
+        # pair counts are whole numbers; rupture times are whole steps
+        floor = {"ruptured_pairs": 1e-2, "rupture_time_steps": 0.5}.get(k, 1e-9)
+        assert ours <= max(floor, 10.0 * own), (k, ours, own)
+
+
+def _against_sensitivity(ref, pert, gpu):
+    fl, fp, fg = _fields(ref), _fields(pert), _fields(gpu)
+    scale = max(np.linalg.norm(fl["slip_rate"]), np.linalg.norm(fl["peak_rate"]))
+    rep = {}
+    for k in fl:
+        sc = scale if k == "slip_rate" else None
+        rep[k] = (_rel(fg[k], fl[k], sc), _rel(fp[k], fl[k], sc))
+    n = ref.npair
+    count = lambda c: int((c.arrays["fnft"][:n] < 1e4).sum())
+    rep["ruptured_pairs"] = (abs(count(gpu) - count(ref)) / count(ref), abs(count(pert) - count(ref)) / count(ref))
+    tr, tp, tg = (c.arrays["fnft"][:n] for c in (ref, pert, gpu))
+    both = (tr < 1e4) & (tp < 1e4) & (tg < 1e4)
+    dt = ref.scalars.dt
+    # mean rupture-time difference in steps, over pairs ruptured in all three runs
+    rep["rupture_time_steps"] = (float(np.abs(tg[both] - tr[both]).mean() / dt), float(np.abs(tp[both] - tr[both]).mean() / dt))
+    return rep
+
+
+def test_c3_fp32_learned(c3):
     from eqdyna_gb300.solver import GpuSolver
     from test_gpu_fp32 import _check, _errors
-    case, cpu, _ = c3
+    case, early, _, late, pert = c3
     with GpuSolver(case.clone(), precision="fp64") as plain:
-        plain.newton_log(NSTEPS)
-        plain.step(NSTEPS)
+        plain.newton_log(N_LATE // 4, 4)
+        plain.step(N_LATE)
         hist = plain.train_mlp(epochs=10, batch=1024, lr=2e-3, holdout=0.1, seed=3)
         params, norm = plain.mlp_state()
         counts = (plain.replay(learned=False), plain.replay(learned=True))
     print("loss", hist, "iterations plain / learned", counts)
+    assert counts[1]["records"] == (N_LATE // 4) * case.npair
     gpu = case.clone()
     with GpuSolver(gpu, precision="fp32") as s:
         s.set_mlp(params, norm)
-        s.step(NSTEPS)
+        s.step(N_EARLY)
         s.fetch()
-        used = s.newton_counts()["learned"]
-    err = _errors(cpu, gpu)
-    print("fp32+learned", err)
-    assert used == NSTEPS * case.npair
-    assert (cpu.arrays["fnft"][: case.npair] < 1e4).sum() > 500  # the rupture is under way
-    _check(err)
+        err = _errors(early, gpu)
+        print("fp32+learned before take-off", err)
+        _check(err)
+        s.step(N_LATE - N_EARLY)
+        s.fetch()
+        nc = s.newton_counts()
+    assert nc["learned"] == N_LATE * case.npair
+    err = _errors(late, gpu)
+    rep = _against_sensitivity(late, pert, gpu)
+    print("fp32+learned after the rupture", err, "repeated solves", nc["fallbacks"])
+    print("binary32 + learned: gpu vs oracle, oracle perturbed by 1e-14 vs oracle:", rep)
+    assert (late.arrays["fnft"][: case.npair] < 1e4).mean() > 0.9  # the rupture crossed the fault
+    assert err["slip"] <= 1e-2 and err["peak_rate"] <= 1e-2
