@@ -160,6 +160,66 @@ def config_c1(path, scale=1.0, nsteps=4000, npml=None):
     return path
 
 
+def c2_layers(dz):
+    """1-D layered medium of C2, one row per cell of thickness dz down to 8 km (as the reference's
+    drv.a6 compset builds its profile): Vs from 1500 m/s at the surface to 3500 m/s at 8 km
+    (linear in depth at the cell centre), Vp = 1.73 Vs, Gardner density rho = 1741 Vp^0.25
+    (kg/m^3, Vp in km/s); rows [depth of the layer bottom, Vp, Vs, rho], the last extended to
+    1000 km."""
+    rows = []
+    i = 0
+    while True:
+        zc = (i + 0.5) * dz
+        vs = 1500.0 + 2000.0 * min(zc / 8.0e3, 1.0)
+        vp = 1.73 * vs
+        rho = 1741.0 * (vp / 1000.0) ** 0.25
+        rows.append([zc + 0.5 * dz, vp, vs, rho])
+        i += 1
+        if zc > 8.0e3:
+            break
+    rows[-1][0] = 1.0e6
+    return np.array(rows)
+
+
+def config_c2(path, scale=1.0, nsteps=6000, q=2, plastic=True):
+    """C2: the C0 box at dx = 50 m (600 x 400 x 300 = 72 M elements + 6-layer PML) in the layered
+    medium of c2_layers; Q with 8 coarse-grained mechanisms, Qs = 50 Vs (km/s), Qp = 2 Qs
+    (C_Q = 2, an extension: the reference's Q is Qs = 10 / 50 by depth and stops with plasticity);
+    Drucker-Prager plasticity (cohesion 1 MPa, bulk friction 0.75, tv = 2 dz / 3464 = 0.029 s at
+    50 m, gravity and the reference's regional stress: principal stress at 45 degrees to the fault,
+    deviatoric / vertical 0.33, hydrostatic pore pressure with overpressure 0.66); slip weakening
+    (mu_s 0.70, mu_d 0.50, Dc 0.3 m, sigma_n = -100 MPa) with tau0 = 60 MPa (1 + 0.1 f), f a seeded
+    von Karman field (correlation length 2 km, Hurst 0.8), and a 3 x 3 km patch at 72 MPa around
+    (0, -7.5 km).  q = 1 selects the reference's Q (then plastic must be False), q = 0 no Q."""
+    if q == 1 and plastic:
+        raise ValueError("the reference's Q (C_Q = 1) does not run with plasticity")
+    p = _base_params()
+    dx = 50.0 * scale
+    layers = c2_layers(dx)
+    p.update(dx=dx, dy=dx, dz=dx, dt=0.002 * scale, friclaw=1, tpv=0, C_nuclea=0,
+             C_elastic=0 if plastic else 1, nmat=len(layers), n2mat=4, roumax=float(layers[-1, 3]),
+             rhow=1000.0, gamar=0.66, bulk=0.75, coheplas=1.0e6, vmaxPML=float(layers[-1, 1]))
+    p["term"] = nsteps * p["dt"]
+    rng = np.random.default_rng(SEED0 + 2)
+    fx, fz = _fault_grid(p)
+    field = von_karman_field(rng, len(fz), len(fx), dx, 2.0e3, 0.8)
+    ofv = np.zeros((24, len(fz), len(fx)))
+    F = _NC_INDEX
+    for ix, x in enumerate(fx):
+        for iz, z in enumerate(fz):
+            edge = abs(abs(x) - p["fxmax"]) < 0.01 or abs(z - p["fzmin"]) < 0.01
+            ofv[F[1], iz, ix] = 1000.0 if edge else 0.70
+            ofv[F[2], iz, ix] = 0.50
+            ofv[F[3], iz, ix] = 0.30
+            ofv[F[7], iz, ix] = -100.0e6
+            patch = abs(x) <= 1.5e3 + 1e-6 and abs(z + 7.5e3) <= 1.5e3 + 1e-6
+            ofv[F[8], iz, ix] = 72.0e6 if patch else 60.0e6 * (1.0 + 0.1 * field[iz, ix])
+    st_on, st_off = _stations(rng, p)
+    write_case_dir(path, p, layers, st_on, st_off, ofv,
+                   gpu_switches={"nPML": 6, "C_hg": 1, "kapa_hg": 0.1, "C_Q": int(q)})
+    return path
+
+
 def config_c3(path, scale=1.0, nsteps=5000, L=0.2, patch_ratio=0.75, patch_radius=2.0e3):
     """30-degree dipping reverse fault reaching the free surface (down-dip width 20 km, 40 km along
     strike), as the reference builds dipping faults (case_input/test.tpv36): cells of dx along
@@ -275,10 +335,12 @@ def config_c4(path, member, nsteps=1500):
     return path
 
 
-CONFIGS = {"C0": config_c0, "C1": config_c1, "C3": config_c3}
+CONFIGS = {"C2": config_c2, "C0": config_c0, "C1": config_c1, "C3": config_c3}
 
 WORKLOADS = {
     "C0": "slip-weakening half-space, dx 200 m, 1,469,664 elements (6-layer PML)",
+    "C2": "layered medium (Vs 1.5-3.5 km/s), Q = 50 Vs with 8 mechanisms, Drucker-Prager plasticity, "
+          "von Karman initial shear stress, slip weakening, dx 50 m",
     "C3": "30-degree dipping reverse fault to the surface, wedge elements along the fault, slip law, "
           "dx 100 m along strike and dip, learned Newton guess",
     "C4": "ensemble of 64 slip-weakening scenarios, dx from {200, 250, 300, 400} m, von Karman initial "

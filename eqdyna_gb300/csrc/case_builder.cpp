@@ -306,7 +306,8 @@ void read_inputs(const std::string &dir, Inputs &in) {
   }
   // option compatibility, src/warning.f90:6-19
   if (in.C_elastic == 0 && in.C_Q == 1) fail("Q model can only work with elastic code");
-  if (in.C_Q == 1 && in.rat > 1) fail("Q model can only work with uniform element size");
+  if (in.C_Q != 0 && in.rat > 1) fail("Q model can only work with uniform element size");
+  if (in.C_Q < 0 || in.C_Q > 2) fail("C_Q must be 0, 1 or 2");
   if (in.output_plastic == 1 && in.C_elastic != 0) fail("plastic strain output needs C_elastic == 0");
   if (in.mode == 2) fail("mode 2 (cycle restart from fault.r.nc) is not built", EQD_ERR_UNSUPPORTED);
   if (in.nPML < 1) fail("nPML must be >= 1 (fixed boundary nodes must be PML nodes)");

@@ -318,6 +318,7 @@ int validate(const eqd_scalars *s, const eqd_host_arrays *a) {
   if (s->friclaw < 1 || s->friclaw > 5) return EQD_ERR_INPUT;
   // the reference stops on Q with plasticity (src/warning.f90:6-9, stop 1001)
   if (s->C_Q == 1 && s->C_elastic == 0) return EQD_ERR_UNSUPPORTED;
+  if (s->C_Q < 0 || s->C_Q > 2) return EQD_ERR_INPUT;
   return EQD_OK;
 }
 
@@ -465,7 +466,7 @@ int build_device_state(eqd_context &X, const eqd_scalars &s, const eqd_host_arra
   if (c.fp32) {
     // Q memory variables in the binary32 form: record-indexed tables only (the Q constants are
     // part of an element's record)
-    if (s.C_Q == 1 && c.opt.table_layout == EQD_TABLES_STREAMED) return EQD_ERR_UNSUPPORTED;
+    if (s.C_Q != 0 && c.opt.table_layout == EQD_TABLES_STREAMED) return EQD_ERR_UNSUPPORTED;
     const int ts = c.opt.tile_shape > 0 ? c.opt.tile_shape : (4 | 8 << 8 | 4 << 16);
     const int bx = ts & 255, by = (ts >> 8) & 255, bz = (ts >> 16) & 255;
     brick_order(a, X.gi_orig, bx, bz, by);
@@ -481,7 +482,7 @@ int build_device_state(eqd_context &X, const eqd_scalars &s, const eqd_host_arra
     if (m == 0) continue;
     std::vector<int> conn(8 * (size_t)m);
     std::vector<double> shp(24 * (size_t)m), phi(32 * (size_t)m), ss(6 * (size_t)m), detw(m), lam(m), mu(m);
-    const int nstress = grp == 0 ? (s.C_Q == 1 ? 12 : 6) : 15;
+    const int nstress = grp == 0 ? (s.C_Q != 0 ? 12 : 6) : 15;
     std::vector<double> st(nstress * (size_t)m), st0, pab, em, hg, porep, pstr, qc;
     bool any_s0 = false;
     int s0_any = 0;
@@ -489,7 +490,7 @@ int build_device_state(eqd_context &X, const eqd_scalars &s, const eqd_host_arra
     if (body) em.assign(8 * (size_t)m, 0.0);
     if (s.C_hg == 2) hg.assign(m, 0.0);
     if (grp == 0 && s.C_elastic == 0) porep.assign(m, 0.0), pstr.assign(m, 0.0);
-    if (grp == 0 && s.C_Q == 1) qc.assign(5 * (size_t)m, 0.0);
+    if (grp == 0 && s.C_Q != 0) qc.assign(5 * (size_t)m, 0.0);
     int bad_ = EQD_OK;
 #pragma omp parallel for schedule(static) reduction(|| : s0_any)
     for (int i = 0; i < m; ++i) {
@@ -539,9 +540,11 @@ int build_device_state(eqd_context &X, const eqd_scalars &s, const eqd_host_arra
           porep[i] = a.eleporep ? a.eleporep[e] : 0.0;
           pstr[i] = a.pstrain ? a.pstrain[e] : 0.0;
         }
-        if (grp == 0 && s.C_Q == 1) {
-          // Q zone and mechanism index from the element centre (src/calcElemKU.f90:78-103)
-          const double Qs = ctr[2] > -1000.0 ? 10.0 : 50.0, Qp = 2.0 * Qs;
+        if (grp == 0 && s.C_Q != 0) {
+          // Q zone and mechanism index from the element centre (src/calcElemKU.f90:78-103); C_Q = 2
+          // (extension): Qs = 50 Vs (km/s), Qp = 2 Qs
+          const double Qs = s.C_Q == 2 ? 50.0 * a.mat[1 * (size_t)ne + e] / 1000.0 : (ctr[2] > -1000.0 ? 10.0 : 50.0);
+          const double Qp = 2.0 * Qs;
           const int ip = (int)((ctr[0] - (s.PMLb[1] + s.dx / 2)) / s.dx + 1);
           const int iq = (int)((ctr[1] - (s.PMLb[3] + s.dx / 2)) / s.dx + 1);
           const int ir = (int)((ctr[2] - (s.PMLb[4] + s.dx / 2)) / s.dx + 1);
@@ -575,7 +578,7 @@ int build_device_state(eqd_context &X, const eqd_scalars &s, const eqd_host_arra
       // record-indexed layout: one record per distinct binary32 (geometry, material) combination
       const int layout = c.opt.table_layout;
       bool use_rec = layout != EQD_TABLES_STREAMED;
-      const bool qm = grp == 0 && s.C_Q == 1;
+      const bool qm = grp == 0 && s.C_Q != 0;
       RecordDict dict(record_length(s.C_hg, body, qm));
       std::vector<unsigned> rid, abid;
       std::vector<float> abt;
@@ -990,12 +993,10 @@ int eqd_gpu_init(const eqd_scalars *s, const eqd_host_arrays *a, const eqd_optio
   return EQD_OK;
 }
 
-int eqd_gpu_step(eqd_context *X, int32_t nt_begin, int32_t nsteps) {
-  if (!X) return EQD_ERR_STATE;
-  if (nsteps < 0 || nt_begin < 1) return EQD_ERR_INPUT;
-  if (nsteps == 0) return EQD_OK;
+namespace {
+// Queues nsteps steps from nt_begin on the context's stream.
+int enqueue_steps(eqd_context *X, int32_t nt_begin, int32_t nsteps, int64_t &launches_out) {
   Context &c = X->c;
-  cudaSetDevice(c.device);
   RC(ensure_times(*X, nt_begin + nsteps));
   if (nt_begin != c.nt + 1) {
     const int prev = nt_begin - 1;
@@ -1028,6 +1029,22 @@ int eqd_gpu_step(eqd_context *X, int32_t nt_begin, int32_t nsteps) {
     RC(launch_step(c));
     launches += per_step;
   }
+  EQD_CUDA_OK(cudaGetLastError());
+  launches_out = launches;
+  return EQD_OK;
+}
+
+int err_status(int err) { return (err & 2) ? EQD_ERR_TIMEOUT : (err ? EQD_ERR_NAN : EQD_OK); }
+}  // namespace
+
+int eqd_gpu_step(eqd_context *X, int32_t nt_begin, int32_t nsteps) {
+  if (!X) return EQD_ERR_STATE;
+  if (nsteps < 0 || nt_begin < 1) return EQD_ERR_INPUT;
+  if (nsteps == 0) return EQD_OK;
+  Context &c = X->c;
+  cudaSetDevice(c.device);
+  int64_t launches = 0;
+  RC(enqueue_steps(X, nt_begin, nsteps, launches));
   EQD_CUDA_OK(cudaStreamSynchronize(c.stream));
   EQD_CUDA_OK(cudaGetLastError());
   int err = 0;
@@ -1037,9 +1054,84 @@ int eqd_gpu_step(eqd_context *X, int32_t nt_begin, int32_t nsteps) {
   c.time = X->times[c.nt];
   c.launches_last = launches;
   c.elem_updates += (int64_t)c.nelem * nsteps;
-  if (err & 2) return EQD_ERR_TIMEOUT;
-  if (err) return EQD_ERR_NAN;
+  return err_status(err);
+}
+
+int eqd_gpu_step_async(eqd_context *X, int32_t nt_begin, int32_t nsteps) {
+  if (!X) return EQD_ERR_STATE;
+  if (nsteps < 0 || nt_begin < 1) return EQD_ERR_INPUT;
+  if (nsteps == 0) return EQD_OK;
+  Context &c = X->c;
+  if (c.profile) return EQD_ERR_STATE;  // profiling accumulates event times at every step call
+  cudaSetDevice(c.device);
+  int64_t launches = 0;
+  RC(enqueue_steps(X, nt_begin, nsteps, launches));
+  c.nt += nsteps;
+  c.time = X->times[c.nt];
+  c.launches_last = launches;
+  c.elem_updates += (int64_t)c.nelem * nsteps;
   return EQD_OK;
+}
+
+int eqd_gpu_fetch_fric_rows_async(eqd_context *X, const int32_t *rows, int32_t nrows, double *dst,
+                                  int64_t *ticket) {
+  if (!X) return EQD_ERR_STATE;
+  if (nrows < 1 || !rows || !dst || !ticket) return EQD_ERR_INPUT;
+  Context &c = X->c;
+  const int np = c.npair;
+  for (int r = 0; r < nrows; ++r)
+    if (rows[r] < 1 || rows[r] > 100) return EQD_ERR_INPUT;
+  cudaSetDevice(c.device);
+  if (!c.copy_stream) {
+    EQD_CUDA_OK(cudaStreamCreateWithFlags(&c.copy_stream, cudaStreamNonBlocking));
+    for (int k = 0; k < 2; ++k) {
+      EQD_CUDA_OK(cudaEventCreateWithFlags(&c.ev_staged[k], cudaEventDisableTiming));
+      EQD_CUDA_OK(cudaEventCreateWithFlags(&c.ev_copied[k], cudaEventDisableTiming));
+    }
+    EQD_CUDA_OK(cudaHostAlloc(reinterpret_cast<void **>(&c.h_err), 2 * sizeof(int), cudaHostAllocDefault));
+    c.h_err[0] = c.h_err[1] = 0;
+  }
+  const int slot = (int)(c.async_issued & 1);
+  // the slot's previous read must have reached the host before the slot is reused
+  if (c.async_issued - c.async_waited >= 2) {
+    EQD_CUDA_OK(cudaEventSynchronize(c.ev_copied[slot]));
+    c.async_waited = c.async_issued - 1;
+  }
+  const size_t need = (size_t)nrows * np + 1;  // rows, then the error word
+  if (c.stage_cap[slot] < need) {
+    EQD_CUDA_OK(cudaEventSynchronize(c.ev_copied[slot]));
+    if (c.d_stage[slot]) cudaFree(c.d_stage[slot]);
+    c.d_stage[slot] = nullptr;
+    if (cudaMalloc(reinterpret_cast<void **>(&c.d_stage[slot]), need * sizeof(double)) != cudaSuccess)
+      return EQD_ERR_OOM;
+    c.stage_cap[slot] = need;
+  }
+  double *st = c.d_stage[slot];
+  EQD_CUDA_OK(cudaStreamWaitEvent(c.stream, c.ev_copied[slot], 0));
+  for (int r = 0; r < nrows; ++r)
+    EQD_CUDA_OK(cudaMemcpyAsync(st + (size_t)r * np, c.fric + (size_t)(rows[r] - 1) * np, np * sizeof(double),
+                                cudaMemcpyDeviceToDevice, c.stream));
+  int *st_err = reinterpret_cast<int *>(st + (size_t)nrows * np);
+  EQD_CUDA_OK(cudaMemcpyAsync(st_err, c.d_err, sizeof(int), cudaMemcpyDeviceToDevice, c.stream));
+  EQD_CUDA_OK(cudaEventRecord(c.ev_staged[slot], c.stream));
+  EQD_CUDA_OK(cudaStreamWaitEvent(c.copy_stream, c.ev_staged[slot], 0));
+  if (np > 0)
+    EQD_CUDA_OK(cudaMemcpyAsync(dst, st, (size_t)nrows * np * sizeof(double), cudaMemcpyDeviceToHost, c.copy_stream));
+  EQD_CUDA_OK(cudaMemcpyAsync(c.h_err + slot, st_err, sizeof(int), cudaMemcpyDeviceToHost, c.copy_stream));
+  EQD_CUDA_OK(cudaEventRecord(c.ev_copied[slot], c.copy_stream));
+  *ticket = c.async_issued++;
+  return EQD_OK;
+}
+
+int eqd_gpu_fetch_wait(eqd_context *X, int64_t ticket) {
+  if (!X) return EQD_ERR_STATE;
+  Context &c = X->c;
+  if (ticket < 0 || ticket >= c.async_issued || ticket < c.async_issued - 2) return EQD_ERR_INPUT;
+  cudaSetDevice(c.device);
+  const int slot = (int)(ticket & 1);
+  EQD_CUDA_OK(cudaEventSynchronize(c.ev_copied[slot]));
+  if (ticket + 1 > c.async_waited) c.async_waited = ticket + 1;
+  return err_status(c.h_err[slot]);
 }
 
 int eqd_gpu_fetch_fault(eqd_context *X, double *fric, double *fnft) {
@@ -1104,7 +1196,9 @@ int eqd_gpu_fetch(eqd_context *X, eqd_host_arrays *a) {
   auto get32 = [&](std::vector<double> &dst, const float *src) -> int {
     std::vector<float> t(dst.size());
     if (!t.empty() && cudaMemcpy(t.data(), src, t.size() * 4, cudaMemcpyDeviceToHost) != cudaSuccess) return EQD_ERR_CUDA;
-    for (size_t q = 0; q < t.size(); ++q) dst[q] = t[q];
+    const long long nt = (long long)t.size();
+#pragma omp parallel for schedule(static)
+    for (long long q = 0; q < nt; ++q) dst[q] = t[q];
     return EQD_OK;
   };
   if (c.fp32) {
@@ -1135,6 +1229,8 @@ int eqd_gpu_fetch(eqd_context *X, eqd_host_arrays *a) {
     }
   }
   auto eq = [&](int j, int k) { return a->eqNumIndexArr[a->eqNumStartIndexLoc[j] + k - 1]; };
+  // every device node d writes only the entries of its own Fortran node j
+#pragma omp parallel for schedule(static)
   for (int d = 0; d < nn; ++d) {
     const int j = X->node_orig[d];
     for (int k = 0; k < 3; ++k) {
@@ -1165,18 +1261,20 @@ int eqd_gpu_fetch(eqd_context *X, eqd_host_arrays *a) {
       const std::vector<int> &ids = grp == 0 ? X->gi_orig : X->gp_orig;
       const int m = (int)ids.size();
       if (m == 0) continue;
-      const int nstress = grp == 0 ? (c.sc.C_Q == 1 ? 12 : 6) : 15;
+      const int nstress = grp == 0 ? (c.sc.C_Q != 0 ? 12 : 6) : 15;
       std::vector<double> st(nstress * (size_t)m);
       if (c.fp32) {
         const ElemGroup<float> &g = grp == 0 ? c.gi32 : c.gp32;
         std::vector<float> s32(nstress * (size_t)g.ld);
         EQD_CUDA_OK(cudaMemcpy(s32.data(), g.stress, s32.size() * 4, cudaMemcpyDeviceToHost));
-        for (int q = 0; q < nstress; ++q)
-          for (int i = 0; i < m; ++i) st[q * (size_t)m + i] = s32[q * (size_t)g.ld + i];
+#pragma omp parallel for schedule(static)
+        for (int i = 0; i < m; ++i)
+          for (int q = 0; q < nstress; ++q) st[q * (size_t)m + i] = s32[q * (size_t)g.ld + i];
       } else {
         const ElemGroup<double> &g = grp == 0 ? c.gi64 : c.gp64;
         EQD_CUDA_OK(cudaMemcpy(st.data(), g.stress, st.size() * 8, cudaMemcpyDeviceToHost));
       }
+#pragma omp parallel for schedule(static)
       for (int i = 0; i < m; ++i) {
         const int64_t base = a->stressCompIndexArr[ids[i]];
         for (int q = 0; q < nstress; ++q) a->stressArr[base + q] = st[q * (size_t)m + i];
@@ -1188,6 +1286,7 @@ int eqd_gpu_fetch(eqd_context *X, eqd_host_arrays *a) {
   if (a->pstrain && dps) {
     std::vector<double> ps(nps);
     EQD_CUDA_OK(cudaMemcpy(ps.data(), dps, ps.size() * 8, cudaMemcpyDeviceToHost));
+#pragma omp parallel for schedule(static)
     for (int i = 0; i < nps; ++i) a->pstrain[X->gi_orig[i]] = ps[i];
   }
   RC(eqd_gpu_fetch_fault(X, a->fric, a->fnft));
@@ -1216,6 +1315,16 @@ int eqd_gpu_finalize(eqd_context *X) {
   if (c.stream) cudaStreamSynchronize(c.stream);
   if (c.graph) cudaGraphExecDestroy(c.graph);
   for (cudaEvent_t e : c.prof_events) cudaEventDestroy(e);
+  if (c.copy_stream) {
+    cudaStreamSynchronize(c.copy_stream);
+    cudaStreamDestroy(c.copy_stream);
+  }
+  for (int k = 0; k < 2; ++k) {
+    if (c.ev_staged[k]) cudaEventDestroy(c.ev_staged[k]);
+    if (c.ev_copied[k]) cudaEventDestroy(c.ev_copied[k]);
+    if (c.d_stage[k]) cudaFree(c.d_stage[k]);
+  }
+  if (c.h_err) cudaFreeHost(c.h_err);
   mlp_free(c);
   for (void *p : c.allocs) cudaFree(p);
   if (c.stream) cudaStreamDestroy(c.stream);

@@ -145,6 +145,14 @@ struct Context {
   double prof_ms[5] = {0, 0, 0, 0, 0};
   int64_t prof_launches[5] = {0, 0, 0, 0, 0};
   std::vector<void *> allocs;   // every device allocation of the context
+  // pipelined result reads (eqd_gpu_fetch_fric_rows_async): two staging slots, each a device copy
+  // of the requested fric rows and the error word, copied to the host on copy_stream
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t ev_staged[2] = {nullptr, nullptr}, ev_copied[2] = {nullptr, nullptr};
+  double *d_stage[2] = {nullptr, nullptr};
+  size_t stage_cap[2] = {0, 0};  // doubles
+  int *h_err = nullptr;          // pinned [2]
+  int64_t async_issued = 0, async_waited = 0;
 };
 
 // ---- launchers implemented in the kernel translation units --------------------------------

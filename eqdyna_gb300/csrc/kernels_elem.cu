@@ -380,7 +380,7 @@ int launch_elements(Context &c, cudaStream_t s, int part) {
   if (c.fp32) return launch_elements_f32(c, s, k, part);
   const bool body = (c.sc.rdampm != 0.0) || (c.sc.C_elastic == 0);
   const bool plastic = (c.sc.C_elastic == 0);
-  const bool qm = (c.sc.C_Q == 1);
+  const bool qm = (c.sc.C_Q != 0);
   int rc = EQD_OK;
   if (part != 1) {
   if (qm && plastic) rc = body ? launch_interior_hg<true, true, true>(c, s, k) : launch_interior_hg<false, true, true>(c, s, k);

@@ -310,7 +310,7 @@ struct Variant {
 };
 Variant variant_of(const Context &c) {
   return Variant{(c.sc.rdampm != 0.0) || (c.sc.C_elastic == 0), c.sc.C_elastic == 0, c.gp32.stress0 != nullptr,
-                 c.sc.C_hg == 2 ? 2 : 1, c.sc.C_Q == 1};
+                 c.sc.C_hg == 2 ? 2 : 1, c.sc.C_Q != 0};
 }
 
 template <bool BODY, bool PLASTIC, int HG, bool QM>
@@ -349,6 +349,8 @@ template <int HG>
 int launch_hg(Context &c, cudaStream_t s, const ElemConst32 &k, bool interior) {
   const Variant v = variant_of(c);
   if (interior) {
+    if (v.plastic && v.q)  // plasticity with Q: C_Q = 2 only (the reference stops on C_Q = 1)
+      return v.body ? launch_interior<true, true, HG, true>(c, s, k) : launch_interior<false, true, HG, true>(c, s, k);
     if (v.plastic)
       return v.body ? launch_interior<true, true, HG, false>(c, s, k) : launch_interior<false, true, HG, false>(c, s, k);
     if (v.q)
@@ -380,6 +382,9 @@ template <int HG>
 int launch_batched_hg(const Variant &v, bool interior, const ElemArgs32 *args, const int *start, int n, int tiles,
                       int Mmax, cudaStream_t s) {
   if (interior) {
+    if (v.plastic && v.q)
+      return v.body ? launch_interior_batched<true, true, HG, true>(args, start, n, tiles, Mmax, s)
+                    : launch_interior_batched<false, true, HG, true>(args, start, n, tiles, Mmax, s);
     if (v.plastic)
       return v.body ? launch_interior_batched<true, true, HG, false>(args, start, n, tiles, Mmax, s)
                     : launch_interior_batched<false, true, HG, false>(args, start, n, tiles, Mmax, s);

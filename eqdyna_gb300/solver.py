@@ -48,6 +48,26 @@ class GpuSolver:
             raise N.EqdError(rc, "eqd_gpu_step")
         self.nt += int(nsteps)
 
+    def step_async(self, nsteps=1):
+        """Queue nsteps steps without waiting (errors surface at the next fetch_wait or step)."""
+        self._rc(self.lib.eqd_gpu_step_async(self._h, self.nt + 1, int(nsteps)), "eqd_gpu_step_async")
+        self.nt += int(nsteps)
+
+    def fetch_fric_rows_async(self, rows, out):
+        """Queue the read of fric rows (1-based) after the queued steps into out[len(rows)][npair]
+        (pinned, e.g. a PinnedArray's array); returns the ticket for fetch_wait."""
+        r = np.ascontiguousarray(rows, dtype=np.int32)
+        assert out.shape == (len(r), self.case.npair) and out.dtype == np.float64 and out.flags.c_contiguous
+        t = C.c_int64()
+        self._rc(self.lib.eqd_gpu_fetch_fric_rows_async(self._h, r.ctypes.data_as(N.c_int32_p), len(r),
+                                                        out.ctypes.data_as(N.c_double_p), C.byref(t)),
+                 "eqd_gpu_fetch_fric_rows_async")
+        return t.value
+
+    def fetch_wait(self, ticket):
+        """Wait until read `ticket` is in host memory; raises on a NaN velocity or a device timeout."""
+        self._rc(self.lib.eqd_gpu_fetch_wait(self._h, int(ticket)), "eqd_gpu_fetch_wait")
+
     def run(self):
         self.step(self.case.nstep - self.nt)
 

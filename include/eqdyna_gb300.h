@@ -55,6 +55,9 @@ typedef struct eqd_scalars {
   double slipRateThres;   /* rupture-time threshold (src/faulting.f90:336)                      */
   double fric_tp_h;       /* global TP width used by thermop (src/thermop.f90:23-31)            */
   double time0;           /* timeElapsed before the first step                                   */
+  /* C_Q: 0 elastic, 1 the reference's coarse-grained Q (Qs 10 above 1 km depth, 50 below; Qp = 2 Qs;
+   * not with plasticity, src/warning.f90:6-9), 2 an extension with no reference counterpart:
+   * Qs = 50 Vs (km/s), Qp = 2 Qs, also with plasticity. */
   int32_t C_elastic, C_Q, C_hg, friclaw, TPV, C_nuclea, nucfault, insertFaultType;
   int32_t nPML, nstep, mode, reserved;
 } eqd_scalars;
@@ -161,6 +164,21 @@ int eqd_gpu_fetch_fault(eqd_context *ctx, double *fric, double *fnft);
  * dst[nrows][npair] (pair index fastest), e.g. rows 71-76 = slip, slip rate and peak slip rate.
  * dst may be pinned (eqd_host_alloc) for a direct DMA. */
 int eqd_gpu_fetch_fric_rows(eqd_context *ctx, const int32_t *rows, int32_t nrows, double *dst);
+
+/* No counterpart in the reference: a pipelined time loop, so that the device never waits for the
+ * host between steps.  eqd_gpu_step_async queues the steps and returns at once (errors surface at
+ * the next wait, fetch or synchronous step; not in profiling mode).  eqd_gpu_fetch_fric_rows_async
+ * queues the read of the given fric rows as they stand after every step queued so far: a device
+ * copy into one of two staging slots on the step stream, then the copy to dst (pinned memory from
+ * eqd_host_alloc, so the copy engine overlaps the next steps) on a second stream; *ticket
+ * identifies the read.  eqd_gpu_fetch_wait blocks until read `ticket` has reached dst and returns
+ * the error status of the steps before it (EQD_ERR_NAN, EQD_ERR_TIMEOUT).  At most two reads are
+ * outstanding: issuing a third first waits for the oldest, whose ticket can then no longer be
+ * waited for (EQD_ERR_INPUT). */
+int eqd_gpu_step_async(eqd_context *ctx, int32_t nt_begin, int32_t nsteps);
+int eqd_gpu_fetch_fric_rows_async(eqd_context *ctx, const int32_t *rows, int32_t nrows, double *dst,
+                                  int64_t *ticket);
+int eqd_gpu_fetch_wait(eqd_context *ctx, int64_t ticket);
 
 /* Page-locked host memory for the buffers a host program exchanges with the device every step
  * (cudaHostAlloc / cudaFreeHost); NULL or EQD_ERR_CUDA on failure. */

@@ -250,7 +250,16 @@ void calc_elem_ku(Oracle &o, int nel, double elresf[24], double &pstrinc_mag) {
       for (int j = 1; j <= 8; ++j) ctr[i - 1] += v.xc(i, v.conn(j, nel));
     for (double &c : ctr) c = c / 8.0;
     double Qs, Qp;
-    if (ctr[2] > -1000.0) { Qs = 10.0; Qp = 20.0; } else { Qs = 50.0; Qp = 100.0; }
+    if (s.C_Q == 2) {  // extension: Qs = 50 Vs (km/s), Qp = 2 Qs
+      Qs = 50.0 * v.mat(nel, 2) / 1000.0;
+      Qp = 2.0 * Qs;
+    } else if (ctr[2] > -1000.0) {
+      Qs = 10.0;
+      Qp = 20.0;
+    } else {
+      Qs = 50.0;
+      Qp = 100.0;
+    }
     const int ip = (int)((ctr[0] - (s.PMLb[1] + s.dx / 2)) / s.dx + 1);
     const int iq = (int)((ctr[1] - (s.PMLb[3] + s.dx / 2)) / s.dx + 1);
     const int ir = (int)((ctr[2] - (s.PMLb[4] + s.dx / 2)) / s.dx + 1);

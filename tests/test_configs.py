@@ -43,3 +43,20 @@ def test_c4_members_differ():
         tau.append(float(c.fric()[:, 7].std()))
     assert len(dx) >= 2
     assert all(t > 0.0 for t in tau) and len({round(t, 3) for t in tau}) == len(tau)
+
+
+def test_c2_layers_and_switches():
+    import pytest
+    from eqdyna_gb300.case import Case
+    from eqdyna_gb300.configs import c2_layers, config_c2
+    rows = c2_layers(50.0)
+    assert rows.shape[1] == 4 and rows[-1, 0] == 1.0e6
+    assert abs(rows[0, 2] - 1506.25) < 1e-9 and rows[-1, 2] == 3500.0   # Vs at 25 m and below 8 km
+    assert np.allclose(rows[:, 1], 1.73 * rows[:, 2])
+    assert np.all(np.diff(rows[:, 3]) >= 0.0)
+    case = Case.from_dir(config_c2(tempfile.mkdtemp(prefix="eqd_c2_"), scale=8.0, nsteps=4))
+    assert case.scalars.C_Q == 2 and case.scalars.C_elastic == 0
+    vs = case.arrays["mat"].reshape(5, -1)[1]
+    assert vs.min() < 2000.0 and vs.max() == 3500.0
+    with pytest.raises(ValueError):
+        config_c2(tempfile.mkdtemp(prefix="eqd_c2_"), scale=8.0, nsteps=4, q=1, plastic=True)
