@@ -183,6 +183,11 @@ def gpu_lib():
         lib.eqd_gpu_fetch_fric_rows_async.restype = C.c_int
         lib.eqd_gpu_fetch_wait.argtypes = [C.c_void_p, C.c_int64]
         lib.eqd_gpu_fetch_wait.restype = C.c_int
+        lib.eqd_gpu_output_setup.argtypes = [C.c_void_p, C.POINTER(C.c_int32), C.c_int32, C.c_int32, C.c_int32]
+        lib.eqd_gpu_output_setup.restype = C.c_int
+        lib.eqd_gpu_output_drain.argtypes = [C.c_void_p, d_p, d_p, C.c_int32, C.POINTER(C.c_int32),
+                                             C.POINTER(C.c_int32)]
+        lib.eqd_gpu_output_drain.restype = C.c_int
         lib.eqd_host_alloc.argtypes = [C.c_int64]
         lib.eqd_host_alloc.restype = C.c_void_p
         lib.eqd_host_free.argtypes = [C.c_void_p]
@@ -210,7 +215,8 @@ GPU_SYMBOLS = ["eqd_gpu_init", "eqd_gpu_step", "eqd_gpu_fetch", "eqd_gpu_fetch_f
                "eqd_gpu_finalize", "eqd_gpu_status_string", "eqd_gpu_stats", "eqd_gpu_time",
                "eqd_gpu_profile", "eqd_gpu_kernel_time", "eqd_gpu_newton_counts", "eqd_gpu_table_info",
                "eqd_gpu_fetch_fric_rows", "eqd_host_alloc", "eqd_host_free", "eqd_gpu_step_async",
-               "eqd_gpu_fetch_fric_rows_async", "eqd_gpu_fetch_wait",
+               "eqd_gpu_fetch_fric_rows_async", "eqd_gpu_fetch_wait", "eqd_gpu_output_setup",
+               "eqd_gpu_output_drain",
                "eqd_ensemble_create", "eqd_ensemble_step", "eqd_ensemble_destroy", "eqd_ensemble_time",
                "eqd_gpu_init_times",
                "eqd_gpu_newton_log", "eqd_gpu_newton_records", "eqd_gpu_mlp_train", "eqd_gpu_mlp_get",

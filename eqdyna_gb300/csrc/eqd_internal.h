@@ -44,6 +44,9 @@ struct ElemGroup {
   // tiles (binary32 form): consecutive runs of `tile` elements of a spatially compact brick
   // order; each tile lists its distinct nodes and, per node, the (element, corner) incidences
   int tile = 0, ntiles = 0, max_tile_nodes = 0;
+  int ne_live = 0;                  // elements (ne counts the slots, empty padding slots included)
+  int *tile_ne = nullptr;           // [ntiles] elements of each tile: its first slots; the rest
+                                    // are empty slots that align the next tile with a brick
   int ld = 0;                       // SoA stride of the binary32 tables: ntiles * tile (padded)
   int *tile_node_ptr = nullptr;     // [ntiles + 1] offsets into tile_nodes
   int *tile_nodes = nullptr;        // device node ids, sorted, per tile
@@ -153,12 +156,19 @@ struct Context {
   size_t stage_cap[2] = {0, 0};  // doubles
   int *h_err = nullptr;          // pinned [2]
   int64_t async_issued = 0, async_waited = 0;
+  // output streams (eqd_gpu_output_setup): a ring of frames written on the device
+  int out_nsurf = 0, out_every = 0, out_ring = 0;
+  int *out_surf = nullptr;       // device node ids of the surface nodes
+  double *out_frames = nullptr;  // [out_ring][3 out_nsurf + npair]
+  int *out_count = nullptr;      // frames written so far (device)
+  int64_t out_drained = 0;       // frames handed to the host
 };
 
 // ---- launchers implemented in the kernel translation units --------------------------------
 int launch_node_update(Context &c, cudaStream_t s);
 int launch_elements(Context &c, cudaStream_t s, int part = 2);  // 0 interior, 1 PML, 2 both
 int launch_fault(Context &c, cudaStream_t s);
+int launch_output_capture(Context &c, cudaStream_t s);
 
 // Ensembles: one launch per kernel over several contexts.  *_update builds the device argument
 // tables on the first call (handle == null) and refreshes them afterwards (per-member state such

@@ -88,6 +88,7 @@ __global__ void __launch_bounds__(kTile)
   unsigned short *sinc = ts.sinc, *slot_of = ts.slot_of;
   float *sv = ts.sv, *sd = ts.sd;
   const int tid = threadIdx.x;
+  const int live = g.tile_ne[blockIdx.x];  // elements of this tile (its first slots)
   const int e0 = blockIdx.x * kTile;
   const int ld = g.ld;
   if (tid == 0) {
@@ -109,7 +110,7 @@ __global__ void __launch_bounds__(kTile)
   __syncthreads();
   const int e = e0 + tid;
   float *fs = tab + L::FS * kTile;
-  if (e < g.ne)
+  if (tid < live)
     interior_element<BODY, PLASTIC, HG, false>(SlabSrc<L>{tab, tid}, sv, sd, Mmax, slot_of, tid, k,
                                         PLASTIC ? g.pstrain + e : nullptr, g.stress + e, (size_t)ld, fs);
   __syncthreads();
@@ -130,6 +131,7 @@ __global__ void __launch_bounds__(kTile)
   unsigned short *sinc = ts.sinc, *slot_of = ts.slot_of;
   float *sv = ts.sv, *sd = ts.sd;
   const int tid = threadIdx.x;
+  const int live = g.tile_ne[blockIdx.x];  // elements of this tile (its first slots)
   const int e0 = blockIdx.x * kTile;
   const int ld = g.ld;
   if (tid == 0) {
@@ -153,7 +155,7 @@ __global__ void __launch_bounds__(kTile)
   const int e = e0 + tid;
   float *cfh = tab + L::FS * kTile;
   float *es = tab + L::ES * kTile;
-  if (e < g.ne)
+  if (tid < live)
     pml_element<BODY, S0, HG>(SlabSrc<L>{tab, tid}, sv, sd, Mmax, slot_of, tid, k, g.stress + e, (size_t)ld,
                               es, cfh);
   __syncthreads();

@@ -132,6 +132,7 @@ __device__ __forceinline__ void interior_rec_body(const ElemArgs32 &a, int tile)
   unsigned short *sinc = ts.sinc, *slot_of = ts.slot_of;
   float *sv = ts.sv, *sd = ts.sd;
   const int tid = threadIdx.x;
+  const int live = g.tile_ne[tile];  // elements of this tile (its first slots)
   const int e0 = tile * kTile;
   const int ld = g.ld;
   if (tid == 0) {
@@ -152,7 +153,7 @@ __device__ __forceinline__ void interior_rec_body(const ElemArgs32 &a, int tile)
   __syncthreads();
   const int e = e0 + tid;
   float *fs = tab + L::FS * kTile;
-  if (e < g.ne) {
+  if (tid < live) {
     double *ps = PLASTIC ? g.pstrain + e : nullptr;
     if (UNI) {
       const UniSrc<L> S{a.rp, tab, tid, nullptr, 0, 0u, 0u};
@@ -180,6 +181,7 @@ __device__ __forceinline__ void pml_rec_body(const ElemArgs32 &a, int tile) {
   unsigned short *sinc = ts.sinc, *slot_of = ts.slot_of;
   float *sv = ts.sv, *sd = ts.sd;
   const int tid = threadIdx.x;
+  const int live = g.tile_ne[tile];  // elements of this tile (its first slots)
   const int e0 = tile * kTile;
   const int ld = g.ld;
   if (tid == 0) {
@@ -205,7 +207,7 @@ __device__ __forceinline__ void pml_rec_body(const ElemArgs32 &a, int tile) {
   float *es = tab + L::ES * kTile;
   const float *rec = g.rec;
   const int rlen = g.rec_len;
-  if (e < g.ne) {
+  if (tid < live) {
     const unsigned ab01 = row_u32(tab, L::ABID, tid), ab2 = row_u32(tab, L::ABID + 1, tid);
     if (UNI) {
       const UniSrc<L> S{a.rp, tab, tid, g.ab_tab, g.ab_stride, ab01, ab2};

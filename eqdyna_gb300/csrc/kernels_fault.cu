@@ -111,16 +111,17 @@ struct NodeArgs32 {
   const int *split_slot;
   int f_is_acc;  // used by the batched launch (the single launch selects a template instead)
   int damp;      // rdampk != 0: the element kernels read u + rdampk v instead of u
+  float rdampk32;
 };
 
 // Node update of the binary32 form.  The force sums arrive in binary32 (Kahan-compensated per
 // tile); acceleration, its increment a*dt and the PML split-field velocities are binary32, while
 // velocity and displacement of every node stay binary64 (increments are small against the state,
 // which is accumulated over 10^3 - 10^4 steps).  Two binary64 operations per component (v += dv,
-// u += v dt; a third for u + rdampk v when stiffness damping is on); the conversions between the
-// formats run on the integer pipe (fpconv.cuh).  Split (fault) nodes are updated entirely in
-// binary64.
-template <bool F_IS_ACC>
+// u += v dt; two more for the PML split sum), no binary64 conversion: the conversions between the
+// formats run on the integer pipe (fpconv.cuh) and u + rdampk v is formed in binary32.  Split
+// (fault) nodes are updated entirely in binary64.
+template <bool F_IS_ACC, bool DAMP>
 __device__ __forceinline__ void node_update32_body(const NodeArgs32 &a, int i) {
   double *__restrict__ vel = a.vel;
   double *__restrict__ disp = a.disp;
@@ -133,6 +134,7 @@ __device__ __forceinline__ void node_update32_body(const NodeArgs32 &a, int i) {
   const int nnode = a.nnode, n_int = a.n_int, npml = a.npml, nsplit = a.nsplit;
   const float dt = a.dt;
   const double dtd = a.dtd, rdampk = a.rdampk;
+  const float rdampk32 = a.rdampk32;
   int *__restrict__ d_err = a.d_err;
   float *__restrict__ vel32 = a.vel32;
   float *__restrict__ dl32 = a.dl32;
@@ -172,7 +174,9 @@ __device__ __forceinline__ void node_update32_body(const NodeArgs32 &a, int i) {
       F[c * nnode + i] = 0.f;
       v32[c] = narrow_f64(vn);
       vel32[c * nnode + i] = v32[c];
-      dl32[c * nnode + i] = narrow_f64(a.damp ? fma(rdampk, vn, u) : u);
+      // u + rdampk v for the element kernels, formed in binary32 from the rounded u and v (within
+      // 1.5 units in the last place of the binary32 value, against 0.5 when formed in binary64)
+      dl32[c * nnode + i] = DAMP ? fmaf(rdampk32, v32[c], narrow_f64(u)) : narrow_f64(u);
     }
     if (isnan(v32[0]) || isnan(v32[1]) || isnan(v32[2])) atomicOr(d_err, 1);
     return;
@@ -216,7 +220,7 @@ __device__ __forceinline__ void node_update32_body(const NodeArgs32 &a, int i) {
         F[c * nnode + i] = 0.f;
         v32[c] = narrow_f64(vn);
         vel32[c * nnode + i] = v32[c];
-        dl32[c * nnode + i] = narrow_f64(a.damp ? fma(rdampk, vn, u) : u);
+        dl32[c * nnode + i] = DAMP ? fmaf(rdampk32, v32[c], narrow_f64(u)) : narrow_f64(u);
       }
       if (isnan(v32[0]) || isnan(v32[1]) || isnan(v32[2])) atomicOr(d_err, 1);
       return;
@@ -225,9 +229,9 @@ __device__ __forceinline__ void node_update32_body(const NodeArgs32 &a, int i) {
   if (isnan(v[0]) || isnan(v[1]) || isnan(v[2])) atomicOr(d_err, 1);
 }
 
-template <bool F_IS_ACC>
+template <bool F_IS_ACC, bool DAMP>
 __global__ void __launch_bounds__(kBlockNodeMax) node_update32(NodeArgs32 a) {
-  node_update32_body<F_IS_ACC>(a, blockIdx.x * blockDim.x + threadIdx.x);
+  node_update32_body<F_IS_ACC, DAMP>(a, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // Member of a batch that owns block b: the largest m with start[m] <= b (start: n + 1 prefix sums).
@@ -253,8 +257,13 @@ __global__ void __launch_bounds__(kBlockNode) node_update32_batched(const NodeAr
   }
   __syncthreads();
   const int i = lb * blockDim.x + threadIdx.x;
-  if (a.f_is_acc) node_update32_body<true>(a, i);
-  else node_update32_body<false>(a, i);
+  if (a.f_is_acc) {
+    if (a.damp) node_update32_body<true, true>(a, i);
+    else node_update32_body<true, false>(a, i);
+  } else {
+    if (a.damp) node_update32_body<false, true>(a, i);
+    else node_update32_body<false, false>(a, i);
+  }
 }
 
 struct FaultArgs {
@@ -656,6 +665,7 @@ NodeArgs32 node_args32(const Context &c) {
   a.nsplit = 2 * c.npair;
   a.f_is_acc = c.f_is_acc;
   a.damp = c.sc.rdampk != 0.0;
+  a.rdampk32 = (float)c.sc.rdampk;
   return a;
 }
 
@@ -714,8 +724,13 @@ int launch_node_update(Context &c, cudaStream_t s) {
     c.npml, c.sc.dt, c.d_nt, c.d_err, c.vel32, c.dl32, c.sc.rdampk
   if (c.fp32) {
     const NodeArgs32 a = node_args32(c);
-    if (c.f_is_acc) node_update32<true><<<grid, bn, 0, s>>>(a);
-    else node_update32<false><<<grid, bn, 0, s>>>(a);
+    if (c.f_is_acc) {
+      if (a.damp) node_update32<true, true><<<grid, bn, 0, s>>>(a);
+      else node_update32<true, false><<<grid, bn, 0, s>>>(a);
+    } else {
+      if (a.damp) node_update32<false, true><<<grid, bn, 0, s>>>(a);
+      else node_update32<false, false><<<grid, bn, 0, s>>>(a);
+    }
   } else {
     if (c.f_is_acc) node_update<true, false><<<grid, bn, 0, s>>>(EQD_NODE_ARGS);
     else node_update<false, false><<<grid, bn, 0, s>>>(EQD_NODE_ARGS);
@@ -797,6 +812,46 @@ void node_fault_batch_free(void *handle) {
   delete b;
 }
 
+namespace {
+struct OutputArgs {
+  const double *vel, *fric;
+  const int *surf, *d_nt;
+  double *frames;
+  int *count;
+  int nnode, npair, nsurf, every, ring;
+};
+
+// output_gm + output_src_evol (src/library_output.f90:267-312) of step nt when
+// (nt - 1) % every == 0 (src/driver.f90:30: mod(nt, 10) == 1): frame (nt - 1) / every of the ring
+// gets the velocity of every surface node and fric(47) of every pair.
+__global__ void __launch_bounds__(256) output_capture_kernel(OutputArgs o) {
+  const int nt = *o.d_nt;
+  if (nt < 1 || (nt - 1) % o.every != 0) return;
+  const int f = (nt - 1) / o.every;
+  const size_t len = 3 * (size_t)o.nsurf + o.npair;
+  double *fr = o.frames + (size_t)(f % o.ring) * len;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < o.nsurf) {
+    const int d = o.surf[t];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) fr[3 * t + c] = o.vel[(size_t)c * o.nnode + d];
+  } else if (t < o.nsurf + o.npair) {
+    const int i = t - o.nsurf;
+    fr[3 * (size_t)o.nsurf + i] = o.fric[46 * (size_t)o.npair + i];
+  }
+  if (t == 0) atomicMax(o.count, f + 1);
+}
+}  // namespace
+
+int launch_output_capture(Context &c, cudaStream_t s) {
+  if (!c.out_frames) return EQD_OK;
+  const OutputArgs o{c.vel, c.fric, c.out_surf, c.d_nt, c.out_frames, c.out_count,
+                     c.nnode, c.npair, c.out_nsurf, c.out_every, c.out_ring};
+  const int n = c.out_nsurf + c.npair;
+  if (n > 0) output_capture_kernel<<<(n + 255) / 256, 256, 0, s>>>(o);
+  return cudaGetLastError() == cudaSuccess ? EQD_OK : EQD_ERR_CUDA;
+}
+
 int launch_fault(Context &c, cudaStream_t s) {
   const int nthreads = c.npair + (c.nOffRows > 0 ? c.nOffRows + 1 : 0);
   if (nthreads == 0) return EQD_OK;
@@ -830,7 +885,8 @@ __global__ void fpconv_check_kernel(long long n, unsigned long long seed, unsign
     const double w1 = widen_f32(f), w2 = (double)f;
     const bool okw = __double_as_longlong(w1) == __double_as_longlong(w2) || (isnan(w1) && isnan(w2));
     const unsigned long long g = mix64(h);
-    const unsigned long long e = 880ull + g % 281ull;
+    // exponents around and inside the binary32 range; one draw in four anywhere (0 .. 2047)
+    const unsigned long long e = ((g >> 40) & 3ull) == 0ull ? g % 2048ull : 880ull + g % 281ull;
     unsigned long long frac = mix64(g) & ((1ull << 52) - 1ull);
     const unsigned long long low = 0x1fffffffull;
     switch (k & 7) {

@@ -66,6 +66,37 @@ module eqd_gpu_mod
       import :: c_ptr, c_int
       integer(c_int), value :: status
     end function
+    ! per-step result reads and the pipelined loop
+    integer(c_int) function eqd_gpu_fetch_fric_rows(ctx, rows, nrows, dst) bind(C, name="eqd_gpu_fetch_fric_rows")
+      import :: c_int, c_ptr, c_int32_t
+      type(c_ptr), value :: ctx, rows, dst
+      integer(c_int32_t), value :: nrows
+    end function
+    integer(c_int) function eqd_gpu_step_async(ctx, nt_begin, nsteps) bind(C, name="eqd_gpu_step_async")
+      import :: c_int, c_ptr, c_int32_t
+      type(c_ptr), value :: ctx
+      integer(c_int32_t), value :: nt_begin, nsteps
+    end function
+    integer(c_int) function eqd_gpu_fetch_fric_rows_async(ctx, rows, nrows, dst, ticket) &
+        bind(C, name="eqd_gpu_fetch_fric_rows_async")
+      import :: c_int, c_ptr, c_int32_t, c_int64_t
+      type(c_ptr), value :: ctx, rows, dst
+      integer(c_int32_t), value :: nrows
+      integer(c_int64_t), intent(out) :: ticket
+    end function
+    integer(c_int) function eqd_gpu_fetch_wait(ctx, ticket) bind(C, name="eqd_gpu_fetch_wait")
+      import :: c_int, c_ptr, c_int64_t
+      type(c_ptr), value :: ctx
+      integer(c_int64_t), value :: ticket
+    end function
+    type(c_ptr) function eqd_host_alloc(bytes) bind(C, name="eqd_host_alloc")
+      import :: c_ptr, c_int64_t
+      integer(c_int64_t), value :: bytes
+    end function
+    integer(c_int) function eqd_host_free(p) bind(C, name="eqd_host_free")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: p
+    end function
   end interface
 
 contains

@@ -68,6 +68,25 @@ class GpuSolver:
         """Wait until read `ticket` is in host memory; raises on a NaN velocity or a device timeout."""
         self._rc(self.lib.eqd_gpu_fetch_wait(self._h, int(ticket)), "eqd_gpu_fetch_wait")
 
+    def output_setup(self, surface_nodes, every=10, ring_frames=64):
+        """Capture output_gm / output_src_evol frames on the device every `every` steps (first at
+        step 1) for these Fortran (1-based) surface node numbers."""
+        sn = np.ascontiguousarray(surface_nodes, dtype=np.int32)
+        self._out_nsurf, self._out_ring = len(sn), int(ring_frames)
+        self._rc(self.lib.eqd_gpu_output_setup(self._h, sn.ctypes.data_as(N.c_int32_p), len(sn), int(every),
+                                               int(ring_frames)), "eqd_gpu_output_setup")
+
+    def output_drain(self, max_frames=1 << 30):
+        """(first_step, gm[k][n_surface][3], src_evol[k][npair]) of the frames not drained yet."""
+        cnt, first = C.c_int32(), C.c_int32()
+        n = min(int(max_frames), self._out_ring)  # at most a ring's worth is pending
+        gm = np.zeros((n, self._out_nsurf, 3))
+        src = np.zeros((n, self.case.npair))
+        self._rc(self.lib.eqd_gpu_output_drain(self._h, gm.ctypes.data_as(N.c_double_p),
+                                               src.ctypes.data_as(N.c_double_p), n, C.byref(cnt),
+                                               C.byref(first)), "eqd_gpu_output_drain")
+        return first.value, gm[: cnt.value], src[: cnt.value]
+
     def run(self):
         self.step(self.case.nstep - self.nt)
 

@@ -180,6 +180,21 @@ int eqd_gpu_fetch_fric_rows_async(eqd_context *ctx, const int32_t *rows, int32_t
                                   int64_t *ticket);
 int eqd_gpu_fetch_wait(eqd_context *ctx, int64_t ticket);
 
+/* Output streams on the device.  The reference writes, when mod(nt, 10) == 1
+ * (src/driver.f90:30-33), the velocity of every surface node (output_gm,
+ * src/library_output.f90:267-279) and fric(47, :) of every pair (output_src_evol, :297-312).
+ * eqd_gpu_output_setup makes every step with (nt - 1) % every == 0 write that frame into a ring of
+ * ring_frames frames in device memory, inside the step (captured in the step graph); the
+ * surface nodes are Fortran node numbers (1-based; surfaceNodeIdArr of find_surfaceNodeIdArr,
+ * :246-262).  eqd_gpu_output_drain copies up to max_frames frames not yet drained, oldest first:
+ * gm[k][n_surface][3] and src_evol[k][npair] (either may be NULL), *frames = the count,
+ * *first_step = nt of the first.  Frames overwritten before a drain are skipped (first_step shows
+ * the gap).  Once per context; not in ensembles. */
+int eqd_gpu_output_setup(eqd_context *ctx, const int32_t *surface_nodes, int32_t n_surface, int32_t every,
+                         int32_t ring_frames);
+int eqd_gpu_output_drain(eqd_context *ctx, double *gm, double *src_evol, int32_t max_frames, int32_t *frames,
+                         int32_t *first_step);
+
 /* Page-locked host memory for the buffers a host program exchanges with the device every step
  * (cudaHostAlloc / cudaFreeHost); NULL or EQD_ERR_CUDA on failure. */
 void *eqd_host_alloc(int64_t bytes);

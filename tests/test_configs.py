@@ -60,3 +60,17 @@ def test_c2_layers_and_switches():
     assert vs.min() < 2000.0 and vs.max() == 3500.0
     with pytest.raises(ValueError):
         config_c2(tempfile.mkdtemp(prefix="eqd_c2_"), scale=8.0, nsteps=4, q=1, plastic=True)
+
+
+def test_surface_nodes_follow_find_surface_node_id_arr():
+    from conftest import golden_path
+    from eqdyna_gb300.case import Case
+    from eqdyna_gb300.outputs import _e18, surface_nodes
+    case = Case.from_fixture(golden_path("tpv8"))
+    nodes = surface_nodes(case)
+    xyz = case.arrays["meshCoor"].reshape(-1, 3)
+    assert len(nodes) > 0 and nodes.min() >= 1
+    assert np.all(np.abs(xyz[nodes - 1, 2]) < case.scalars.dx / 1000.0)
+    top = np.flatnonzero(np.abs(xyz[:, 2]) < case.scalars.dx / 1000.0)
+    assert len(top) >= len(nodes)
+    assert _e18(-2.5e-3) == "  -0.2500000E-0002" and _e18(1000.0) == "   0.1000000E+0004"
