@@ -417,7 +417,11 @@ def bench_ours(args, world, rank, local):
                        "learned_guess": bool(args.learned), "scale": args.scale,
                        "l2": f"inputs larger than L2: working set {working_set / 1e9:.2f} GB per step "
                              "vs 129 MB L2, no flush",
-                       "element_tables": {k: (v["layout"], v["records"]) for k, v in tables.items()},
+                       "element_tables": {k: {"layout": v["layout"], "records": v["records"], "tiles": v["tiles"],
+                                              "max_tile_nodes": v["max_tile_nodes"],
+                                              "node_gathers_per_element": round(v["tile_nodes"] / max(v["elements"], 1), 3),
+                                              "live_slots": round(v["elements"] / max(v["slots"], 1), 4)}
+                                          for k, v in tables.items()},
                        "launch": launch or "defaults",
                        "parallelism": "replicas" if world > 1 else "single GPU",
                        "setup_s": round(setup_s, 1), "wall_ms_per_step": wall * 1e3 / args.steps},

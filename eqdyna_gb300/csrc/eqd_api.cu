@@ -244,6 +244,7 @@ int build_tiles(Context &c, ElemGroup<float> &g, const std::vector<int> &conn_de
   g.max_tile_nodes = std::max(maxM, 1);
   g.ne_live = 0;
   for (int t = 0; t < nt; ++t) g.ne_live += tile_ne[t];
+  g.sum_tile_nodes = node_ptr[nt];
   int rc;
   if ((rc = dupload(c, g.tile_ne, tile_ne))) return rc;
   if ((rc = dupload(c, g.tile_node_ptr, node_ptr))) return rc;
@@ -1707,7 +1708,7 @@ int eqd_gpu_init_times(eqd_context *X, double ms[8]) {
   return EQD_OK;
 }
 
-int eqd_gpu_table_info(eqd_context *X, int32_t group, int64_t info[4]) {
+int eqd_gpu_table_info(eqd_context *X, int32_t group, int64_t info[8]) {
   if (!X) return EQD_ERR_STATE;
   if ((group != 0 && group != 1) || !info) return EQD_ERR_INPUT;
   const Context &c = X->c;
@@ -1716,6 +1717,10 @@ int eqd_gpu_table_info(eqd_context *X, int32_t group, int64_t info[4]) {
   info[1] = c.fp32 ? g.ne_live : (group == 0 ? c.gi64.ne : c.gp64.ne);
   info[2] = g.nrec;
   info[3] = g.rec_len;
+  info[4] = c.fp32 ? g.ntiles : 0;
+  info[5] = c.fp32 ? (int64_t)g.ntiles * g.tile : 0;
+  info[6] = c.fp32 ? g.max_tile_nodes : 0;
+  info[7] = c.fp32 ? g.sum_tile_nodes : 0;
   return EQD_OK;
 }
 

@@ -45,6 +45,7 @@ struct ElemGroup {
   // order; each tile lists its distinct nodes and, per node, the (element, corner) incidences
   int tile = 0, ntiles = 0, max_tile_nodes = 0;
   int ne_live = 0;                  // elements (ne counts the slots, empty padding slots included)
+  int64_t sum_tile_nodes = 0;       // distinct nodes summed over the tiles
   int *tile_ne = nullptr;           // [ntiles] elements of each tile: its first slots; the rest
                                     // are empty slots that align the next tile with a brick
   int ld = 0;                       // SoA stride of the binary32 tables: ntiles * tile (padded)

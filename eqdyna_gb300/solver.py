@@ -216,12 +216,13 @@ class GpuSolver:
         record_floats}}; layout is "records", "streamed" or None (empty group / binary64 form)."""
         out = {}
         for name, grp in (("interior", 0), ("pml", 1)):
-            info = (C.c_int64 * 4)()
+            info = (C.c_int64 * 8)()
             rc = self.lib.eqd_gpu_table_info(self._h, grp, info)
             if rc != 0:
                 raise N.EqdError(rc, "eqd_gpu_table_info")
             out[name] = {"layout": {0: None, 1: "streamed", 2: "records"}[info[0]], "elements": info[1],
-                         "records": info[2], "record_floats": info[3]}
+                         "records": info[2], "record_floats": info[3], "tiles": info[4], "slots": info[5],
+                         "max_tile_nodes": info[6], "tile_nodes": info[7]}
         return out
 
     @property

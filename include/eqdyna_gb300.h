@@ -307,8 +307,10 @@ int eqd_gpu_init_times(eqd_context *ctx, double ms[8]);
 
 /* Element-table layout of the binary32 form for group 0 (interior) or 1 (PML):
  * info[0] = 2 record-indexed, 1 streamed, 0 group empty or binary64 form; info[1] = elements;
- * info[2] = distinct records; info[3] = floats per record (both 0 when streamed). */
-int eqd_gpu_table_info(eqd_context *ctx, int32_t group, int64_t info[4]);
+ * info[2] = distinct records; info[3] = floats per record (both 0 when streamed); info[4] = tiles;
+ * info[5] = element slots (tiles x 128, empty slots included); info[6] = most distinct nodes of a
+ * tile; info[7] = distinct nodes summed over the tiles (the node gathers of one pass). */
+int eqd_gpu_table_info(eqd_context *ctx, int32_t group, int64_t info[8]);
 
 /* Measured binary64 fused-multiply-add throughput of a device (TFLOP/s, 2 flops per FMA),
  * from a register-resident FMA chain kernel; used as the compute roofline of the FP64 form. */
