@@ -62,8 +62,8 @@ NODE_BYTES = {"fp64": (152, 536), "fp32": (148, 340)}
 # DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) per element of the binary32
 # kernels on a uniform grid (one record per group), from the ncu capture of C1 at dx = 200 m
 # (profiles/elem_f32_uniform_C1-dx200.md), scaled to a launch by its element count.
-NCU_TRAFFIC_PER_UNIT = {("elem_interior", "records", 1): (105.420032e6 + 10.960384e6) / 1125000,
-                        ("elem_pml", "records", 1): (256.453376e6 + 106.076672e6) / 1402000}
+NCU_TRAFFIC_PER_UNIT = {("elem_interior", "records", 1): (112.008448e6 + 11.831808e6) / 1125000,
+                        ("elem_pml", "records", 1): (283.672832e6 + 106.202880e6) / 1402000}
 JOB_STEPS = {"C0": 1000, "C1": 4000, "C2": 6000, "C3": 5000}
 # the result a host program reads after every step: fric rows 71-76 (slip s/d/n, slip rate s/d,
 # peak slip rate) of every fault pair
@@ -353,8 +353,16 @@ def bench_ours(args, world, rank, local):
     if args.learned:
         s.set_mlp(params, norm)
     s.step(args.warmup)
-    n_before = s.newton_counts()
+    # per-kernel times: CUDA events around every launch over a short segment, issued in the
+    # reference's order (no graph, no overlap); they give the kernel shares and rooflines
     s.profile(True, reset=True)
+    s.step(min(args.steps, 40))
+    s.profile(False)
+    kt = s.kernel_times()
+    # the timed region: the production path (16-step CUDA graphs, the fault phase overlapped with the
+    # next step's node update), CUDA events around the whole call on the library's stream
+    n_before = s.newton_counts()
+    s.profile(True, reset=True, calls_only=True)
     barrier(world)
     with ClockSampler(local) as clk:
         w0 = time.perf_counter()
@@ -362,13 +370,13 @@ def bench_ours(args, world, rank, local):
         wall = time.perf_counter() - w0
     barrier(world)
     s.profile(False)
-    kt = s.kernel_times()
+    timed_ms = s.kernel_times()["step"][0]
     stats = s.stats()
     n_after = s.newton_counts()
     newton = {k: n_after[k] - n_before[k] for k in n_after}
     tables = s.table_info()
     step_ms_total = kt["step"][0]
-    dev_s = allreduce_max(step_ms_total / 1e3, world)
+    dev_s = allreduce_max(timed_ms / 1e3, world)
     units = allreduce_sum(float(ne) * args.steps, world)
     value = units / dev_s
     s.close()
@@ -424,7 +432,11 @@ def bench_ours(args, world, rank, local):
                                           for k, v in tables.items()},
                        "launch": launch or "defaults",
                        "parallelism": "replicas" if world > 1 else "single GPU",
-                       "setup_s": round(setup_s, 1), "wall_ms_per_step": wall * 1e3 / args.steps},
+                       "setup_s": round(setup_s, 1), "wall_ms_per_step": wall * 1e3 / args.steps,
+                       "timing": "value: CUDA events around the K-step call on the library's stream (16-step "
+                                 "graphs, fault phase beside the next node update); kernel shares and "
+                                 "rooflines: per-launch events over up to 40 steps in the reference's order",
+                       "sequential_ms_per_step": round(step_ms_total / max(kt["step"][1], 1), 4)},
             "e2e": {"value": ne * job * world / e2e_s, "unit": UNIT, "steps": job,
                     "h2d_bytes_per_step": int(host_bytes_in / job),
                     "d2h_bytes_per_step": int(d2h_per_step + host_bytes_in / job),

@@ -70,7 +70,7 @@ class EqdOptions(C.Structure):
     _fields_ = [("precision", C.c_int32), ("learned_guess", C.c_int32),
                 ("record_tp_hist", C.c_int32), ("tile_shape", C.c_int32),
                 ("use_graph", C.c_int32), ("device", C.c_int32), ("table_layout", C.c_int32),
-                ("block_node", C.c_int32), ("block_fault", C.c_int32), ("reserved", C.c_int32)]
+                ("block_node", C.c_int32), ("block_fault", C.c_int32), ("sequential_fault", C.c_int32)]
 
 
 PREC_FP64 = 0

@@ -53,7 +53,8 @@ def tuning_path(config, gpu):
 
 
 def measure(case, precision, options, steps=16, warmup=3, device=0):
-    """Device time per step (ms) and per-kernel shares of a fresh context with these options."""
+    """Device time per step (ms, the production path: graphs and the overlapped fault phase) and
+    per-kernel shares (per-launch events, the reference's order) of a fresh context."""
     from .solver import GpuSolver
     with GpuSolver(case.clone(), precision=precision, device=device, **options) as s:
         s.step(warmup)
@@ -61,8 +62,12 @@ def measure(case, precision, options, steps=16, warmup=3, device=0):
         s.step(steps)
         s.profile(False)
         kt = s.kernel_times()
-    total = kt["step"][0]
-    return total / steps, {k: round(v[0] / total, 4) for k, v in kt.items() if k != "step"}
+        s.profile(True, reset=True, calls_only=True)
+        s.step(steps)
+        s.profile(False)
+        total = s.kernel_times()["step"][0]
+    seq = kt["step"][0]
+    return total / steps, {k: round(v[0] / seq, 4) for k, v in kt.items() if k != "step"}
 
 
 def tune(case, precision="fp32", steps=16, warmup=3, device=0, log=print):

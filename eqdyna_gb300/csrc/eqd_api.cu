@@ -35,6 +35,7 @@ struct eqd_context {
   std::vector<int> gi_orig, gp_orig;             // device element slot -> original element
   std::vector<int> pair_station_col;             // on-fault station columns
   std::vector<double> times;                     // timeElapsed after n steps
+  std::vector<unsigned char> split_node;         // device node -> 1 for a split (fault) node
   int nftmx = 0;
 };
 
@@ -465,6 +466,8 @@ int build_device_state(eqd_context &X, const eqd_scalars &s, const eqd_host_arra
         if (d >= c.n_int) return EQD_ERR_UNSUPPORTED;
         slot[d] = 2 * i + k;
         im32[d] = -im32[d];
+        if (X.split_node.empty()) X.split_node.assign(nn, 0);
+        X.split_node[d] = 1;
         for (int q = 0; q < 3; ++q) fsplit[(size_t)q * 2 * npair0 + 2 * i + k] = F[(size_t)q * nn + d];
       }
     RC(dupload(c, c.inv_mass32, im32));
@@ -598,6 +601,13 @@ int build_device_state(eqd_context &X, const eqd_scalars &s, const eqd_host_arra
     }
     if (bad_) return bad_;
     any_s0 = s0_any;
+    if (c.fp32 && grp == 1 && !X.split_node.empty()) {  // does a PML element touch a split node?
+      int touch = 0;
+#pragma omp parallel for schedule(static) reduction(| : touch)
+      for (long long q = 0; q < 8 * (long long)m; ++q)
+        if (conn[q] >= 0 && X.split_node[conn[q]]) touch = 1;
+      c.pml_touches_split = touch;
+    }
     mark(2);
     if (c.fp32) {
       ElemGroup<float> &h = grp == 0 ? c.gi32 : c.gp32;
@@ -843,6 +853,7 @@ int build_device_state(eqd_context &X, const eqd_scalars &s, const eqd_host_arra
   mark(5);
   // ---- step bookkeeping ----
   RC(dalloc(c, c.d_nt, 1));
+  RC(dalloc(c, c.d_nt_c, 1));
   RC(dalloc(c, c.d_err, 1));
   RC(dalloc(c, c.d_stats, 5));
   EQD_CUDA_OK(cudaMemset(c.d_nt, 0, sizeof(int)));
@@ -880,6 +891,59 @@ int ensure_times(eqd_context &X, int last_nt) {
 
 // Events of one profiled step: [start, after node, after interior, after PML, after fault].
 constexpr int kEventsPerStep = 5;
+
+// The overlapped schedule (binary32 form, no per-launch profiling).  The fault phase of step n
+// (thermal pressurization, fault kernel, fric(47) frame) touches only split nodes and fault rows;
+// the bulk node update of step n + 1 touches every other node, and the PML element pass (when no
+// PML element has a split node) reads and adds to non-split nodes only.  So they run side by side:
+// the fault phase on c.side, forked after the interior element pass of step n and joined before the
+// split nodes of step n + 1 are updated.  Per step: bulk node update, PML elements || fault phase of
+// the previous step; split nodes (and the step number for the fault phase); off-fault station
+// rows; surface frame; interior elements.  The last fault phase of a call runs on the main stream,
+// so every call ends with the state of a completed step.
+int launch_steps_overlapped(Context &c, int nsteps) {
+  if (!c.side) {
+    // the fault phase is a short chain of latency-bound launches beside a bandwidth-bound one:
+    // give it the highest priority so that its blocks are placed first as SM slots free up
+    int lo = 0, hi = 0;
+    EQD_CUDA_OK(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+    EQD_CUDA_OK(cudaStreamCreateWithPriority(&c.side, cudaStreamNonBlocking, hi));
+    EQD_CUDA_OK(cudaEventCreateWithFlags(&c.ev_fork, cudaEventDisableTiming));
+    EQD_CUDA_OK(cudaEventCreateWithFlags(&c.ev_join, cudaEventDisableTiming));
+  }
+  for (int k = 0; k < nsteps; ++k) {
+    // the fault phase of the previous step (binary64 transcendentals) is forked after this step's
+    // bulk node update, which needs the binary64 pipe too, so that it runs beside the PML pass
+    const bool fork = k > 0 && !c.pml_touches_split;
+    if (k > 0 && c.pml_touches_split) {
+      EQD_CUDA_OK(cudaEventRecord(c.ev_fork, c.stream));
+      EQD_CUDA_OK(cudaStreamWaitEvent(c.side, c.ev_fork, 0));
+      RC(launch_fault(c, c.side, true));
+      RC(launch_output_capture(c, c.side, 2, true));
+      EQD_CUDA_OK(cudaEventRecord(c.ev_join, c.side));
+    }
+    RC(launch_node_update(c, c.stream, true));
+    if (fork) {
+      EQD_CUDA_OK(cudaEventRecord(c.ev_fork, c.stream));
+      EQD_CUDA_OK(cudaStreamWaitEvent(c.side, c.ev_fork, 0));
+      RC(launch_fault(c, c.side, true));
+      RC(launch_output_capture(c, c.side, 2, true));
+      EQD_CUDA_OK(cudaEventRecord(c.ev_join, c.side));
+    }
+    // the PML elements touch no split node: they run beside the fault phase
+    if (!c.pml_touches_split) RC(launch_elements(c, c.stream, 1));
+    if (k > 0) EQD_CUDA_OK(cudaStreamWaitEvent(c.stream, c.ev_join, 0));
+    RC(launch_split_update(c, c.stream));
+    c.f_is_acc = 0;
+    RC(launch_station_capture(c, c.stream));
+    RC(launch_output_capture(c, c.stream, 1, true));
+    RC(launch_elements(c, c.stream, 0));
+    if (c.pml_touches_split) RC(launch_elements(c, c.stream, 1));
+  }
+  RC(launch_fault(c, c.stream, true));
+  RC(launch_output_capture(c, c.stream, 2, true));
+  return EQD_OK;
+}
 
 int launch_step(Context &c, cudaEvent_t *ev = nullptr) {
   if (ev) EQD_CUDA_OK(cudaEventRecord(ev[0], c.stream));
@@ -942,11 +1006,24 @@ __global__ void fp64_fma_chain(double *out, int iters, double a, double b) {
 
 constexpr int kGraphSteps = 16;
 
+bool overlapped(const Context &c) { return c.fp32 && !c.profile && !c.opt.sequential_fault; }
+
+// Kernel launches of one step (for the launch counters).
+int launches_per_step(const Context &c) {
+  const int elem = (c.gi64.ne > 0 || c.gi32.ne > 0 ? 1 : 0) + (c.gp64.ne > 0 || c.gp32.ne > 0 ? 1 : 0);
+  const int tp = (c.sc.friclaw == 5 && c.tp_hist) ? 1 : 0;
+  const int out = c.out_frames ? 1 : 0;
+  if (!overlapped(c)) return 2 + elem + tp + out;
+  return 3 + elem + tp + (c.nOffRows > 0 && c.offhist ? 1 : 0) + 2 * out;
+}
+
 int build_graph(Context &c) {
   cudaGraph_t g = nullptr;
   EQD_CUDA_OK(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
   int rc = EQD_OK;
-  for (int k = 0; k < kGraphSteps && rc == EQD_OK; ++k) rc = launch_step(c);
+  if (overlapped(c)) rc = launch_steps_overlapped(c, kGraphSteps);
+  else
+    for (int k = 0; k < kGraphSteps && rc == EQD_OK; ++k) rc = launch_step(c);
   cudaError_t e = cudaStreamEndCapture(c.stream, &g);
   if (rc) {
     if (g) cudaGraphDestroy(g);
@@ -1040,7 +1117,8 @@ int enqueue_steps(eqd_context *X, int32_t nt_begin, int32_t nsteps, int64_t &lau
   }
   int done = 0;
   int64_t launches = 0;
-  const int per_step = 3 + (c.gp64.ne > 0 || c.gp32.ne > 0 ? 1 : 0) + (c.sc.friclaw == 5 && c.tp_hist ? 1 : 0);
+  const int per_step = launches_per_step(c);
+  const bool ov = overlapped(c);
   if (c.profile) {
     RC(ensure_events(c, nsteps));
     for (; done < nsteps; ++done) RC(launch_step(c, &c.prof_events[(size_t)kEventsPerStep * done]));
@@ -1048,7 +1126,7 @@ int enqueue_steps(eqd_context *X, int32_t nt_begin, int32_t nsteps, int64_t &lau
   }
   // the first step after init consumes the stored acceleration and runs outside the graph
   if (c.f_is_acc && done < nsteps) {
-    RC(launch_step(c));
+    RC(ov ? launch_steps_overlapped(c, 1) : launch_step(c));
     ++done;
     launches += per_step;
   }
@@ -1059,6 +1137,11 @@ int enqueue_steps(eqd_context *X, int32_t nt_begin, int32_t nsteps, int64_t &lau
       done += kGraphSteps;
       launches += (int64_t)per_step * kGraphSteps;
     }
+  }
+  if (ov && done < nsteps) {
+    RC(launch_steps_overlapped(c, nsteps - done));
+    launches += (int64_t)per_step * (nsteps - done);
+    done = nsteps;
   }
   for (; done < nsteps; ++done) {
     RC(launch_step(c));
@@ -1079,12 +1162,20 @@ int eqd_gpu_step(eqd_context *X, int32_t nt_begin, int32_t nsteps) {
   Context &c = X->c;
   cudaSetDevice(c.device);
   int64_t launches = 0;
+  if (c.time_calls) EQD_CUDA_OK(cudaEventRecord(c.call_ev[0], c.stream));
   RC(enqueue_steps(X, nt_begin, nsteps, launches));
+  if (c.time_calls) EQD_CUDA_OK(cudaEventRecord(c.call_ev[1], c.stream));
   EQD_CUDA_OK(cudaStreamSynchronize(c.stream));
   EQD_CUDA_OK(cudaGetLastError());
   int err = 0;
   EQD_CUDA_OK(cudaMemcpy(&err, c.d_err, sizeof(int), cudaMemcpyDeviceToHost));
   if (c.profile) RC(accumulate_profile(c, nsteps));
+  if (c.time_calls) {
+    float ms = 0.f;
+    EQD_CUDA_OK(cudaEventElapsedTime(&ms, c.call_ev[0], c.call_ev[1]));
+    c.prof_ms[0] += ms;
+    c.prof_launches[0] += nsteps;
+  }
   c.nt += nsteps;
   c.time = X->times[c.nt];
   c.launches_last = launches;
@@ -1421,6 +1512,14 @@ int eqd_gpu_finalize(eqd_context *X) {
     cudaStreamSynchronize(c.copy_stream);
     cudaStreamDestroy(c.copy_stream);
   }
+  if (c.side) {
+    cudaStreamSynchronize(c.side);
+    cudaStreamDestroy(c.side);
+  }
+  if (c.ev_fork) cudaEventDestroy(c.ev_fork);
+  if (c.ev_join) cudaEventDestroy(c.ev_join);
+  for (int k = 0; k < 2; ++k)
+    if (c.call_ev[k]) cudaEventDestroy(c.call_ev[k]);
   for (int k = 0; k < 2; ++k) {
     if (c.ev_staged[k]) cudaEventDestroy(c.ev_staged[k]);
     if (c.ev_copied[k]) cudaEventDestroy(c.ev_copied[k]);
@@ -1458,7 +1557,17 @@ int eqd_gpu_profile(eqd_context *X, int32_t enable) {
     for (int k = 0; k < 5; ++k) c.prof_ms[k] = 0.0, c.prof_launches[k] = 0;
     return EQD_OK;
   }
+  if (enable == 3) {
+    cudaSetDevice(c.device);
+    for (int k = 0; k < 2; ++k)
+      if (!c.call_ev[k]) EQD_CUDA_OK(cudaEventCreate(&c.call_ev[k]));
+    c.profile = 0;
+    c.time_calls = 1;
+    return EQD_OK;
+  }
+  if (enable < 0 || enable > 3) return EQD_ERR_INPUT;
   c.profile = enable ? 1 : 0;
+  c.time_calls = 0;
   return EQD_OK;
 }
 

@@ -128,6 +128,11 @@ struct Context {
   int nlog_nt0 = 0, nlog_steps = 0, nlog_stride = 1;
   // step bookkeeping
   int *d_nt = nullptr;          // current step index on the device
+  int *d_nt_c = nullptr;        // its copy for the fault phase of the overlapped schedule
+  int pml_touches_split = 0;    // a PML element has a split node (the PML pass then waits for
+                                // the split-node update, like the interior pass)
+  cudaStream_t side = nullptr;  // fault phase of the overlapped schedule
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   double *d_times = nullptr;    // [nstep + 2] timeElapsed after nt steps
   int *d_err = nullptr;         // error word: 1 = NaN velocity, 2 = bounded wait gave up
   unsigned long long *d_stats = nullptr;  // [5]: Newton iterations (as counted by the reference),
@@ -145,6 +150,8 @@ struct Context {
   int times_cap = 0;            // entries of d_times
   // profiling (CUDA events around every launch of a step)
   int profile = 0;
+  int time_calls = 0;           // events around each step call only (graphs and overlap kept)
+  cudaEvent_t call_ev[2] = {nullptr, nullptr};
   std::vector<cudaEvent_t> prof_events;
   double prof_ms[5] = {0, 0, 0, 0, 0};
   int64_t prof_launches[5] = {0, 0, 0, 0, 0};
@@ -166,10 +173,12 @@ struct Context {
 };
 
 // ---- launchers implemented in the kernel translation units --------------------------------
-int launch_node_update(Context &c, cudaStream_t s);
+int launch_node_update(Context &c, cudaStream_t s, bool skip_split = false);
 int launch_elements(Context &c, cudaStream_t s, int part = 2);  // 0 interior, 1 PML, 2 both
-int launch_fault(Context &c, cudaStream_t s);
-int launch_output_capture(Context &c, cudaStream_t s);
+int launch_fault(Context &c, cudaStream_t s, bool overlapped = false);
+int launch_output_capture(Context &c, cudaStream_t s, int part = 3, bool overlapped = false);
+int launch_split_update(Context &c, cudaStream_t s);
+int launch_station_capture(Context &c, cudaStream_t s);
 
 // Ensembles: one launch per kernel over several contexts.  *_update builds the device argument
 // tables on the first call (handle == null) and refreshes them afterwards (per-member state such

@@ -112,7 +112,31 @@ struct NodeArgs32 {
   int f_is_acc;  // used by the batched launch (the single launch selects a template instead)
   int damp;      // rdampk != 0: the element kernels read u + rdampk v instead of u
   float rdampk32;
+  int skip_split;  // split nodes are left to split_update32 (overlapped step schedule)
 };
+
+// Split (fault) node i, slot q of Fsplit: the fault kernel set its force in binary64; the update is
+// binary64 so that the slave-master relative motion keeps binary64 resolution (creep rates
+// ~1e-12..1e-16 m/s).
+template <bool F_IS_ACC>
+__device__ __forceinline__ void split_node_update(const NodeArgs32 &a, int i, int q) {
+  const int nnode = a.nnode;
+  const double imd = -(double)a.inv_mass[i];
+  double v[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const double f = a.Fsplit[(size_t)c * a.nsplit + q];
+    const double acc = F_IS_ACC ? f : f * imd;
+    v[c] = fma(acc, a.dtd, a.vel[c * nnode + i]);
+    a.vel[c * nnode + i] = v[c];
+    const double u = fma(v[c], a.dtd, a.disp[c * nnode + i]);
+    a.disp[c * nnode + i] = u;
+    a.F[c * nnode + i] = 0.f;
+    a.vel32[c * nnode + i] = (float)v[c];
+    a.dl32[c * nnode + i] = (float)fma(a.rdampk, v[c], u);
+  }
+  if (isnan(v[0]) || isnan(v[1]) || isnan(v[2])) atomicOr(a.d_err, 1);
+}
 
 // Node update of the binary32 form.  The force sums arrive in binary32 (Kahan-compensated per
 // tile); acceleration, its increment a*dt and the PML split-field velocities are binary32, while
@@ -131,36 +155,21 @@ __device__ __forceinline__ void node_update32_body(const NodeArgs32 &a, int i) {
   float *__restrict__ v9 = a.v9;
   double *__restrict__ vh = a.vh;
   const float *__restrict__ pml_ab = a.pml_ab;
-  const int nnode = a.nnode, n_int = a.n_int, npml = a.npml, nsplit = a.nsplit;
+  const int nnode = a.nnode, n_int = a.n_int, npml = a.npml;
   const float dt = a.dt;
-  const double dtd = a.dtd, rdampk = a.rdampk;
+  const double dtd = a.dtd;
   const float rdampk32 = a.rdampk32;
   int *__restrict__ d_err = a.d_err;
   float *__restrict__ vel32 = a.vel32;
   float *__restrict__ dl32 = a.dl32;
-  const double *__restrict__ Fsplit = a.Fsplit;
   const int *__restrict__ split_slot = a.split_slot;
   if (i == 0) *a.d_nt += 1;
   if (i >= nnode) return;
   const float im = inv_mass[i];
   double v[3];
   if (im < 0.f) {
-    // split (fault) node: the fault kernel set its force in binary64; update it in binary64 so
-    // the slave-master relative motion keeps binary64 resolution (creep rates ~1e-12..1e-16 m/s)
-    const int q = split_slot[i];
-    const double imd = -(double)im;
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      const double f = Fsplit[(size_t)c * nsplit + q];
-      const double acc = F_IS_ACC ? f : f * imd;
-      v[c] = fma(acc, dtd, vel[c * nnode + i]);
-      vel[c * nnode + i] = v[c];
-      const double u = fma(v[c], dtd, disp[c * nnode + i]);
-      disp[c * nnode + i] = u;
-      F[c * nnode + i] = 0.f;
-      vel32[c * nnode + i] = (float)v[c];
-      dl32[c * nnode + i] = (float)fma(rdampk, v[c], u);
-    }
+    if (!a.skip_split) split_node_update<F_IS_ACC>(a, i, split_slot[i]);
+    return;
   } else if (i < n_int) {
     float v32[3];
 #pragma unroll
@@ -666,6 +675,7 @@ NodeArgs32 node_args32(const Context &c) {
   a.f_is_acc = c.f_is_acc;
   a.damp = c.sc.rdampk != 0.0;
   a.rdampk32 = (float)c.sc.rdampk;
+  a.skip_split = 0;
   return a;
 }
 
@@ -717,13 +727,14 @@ FaultArgs fault_args(Context &c) {
 
 }  // namespace
 
-int launch_node_update(Context &c, cudaStream_t s) {
+int launch_node_update(Context &c, cudaStream_t s, bool skip_split) {
   const int bn = c.opt.block_node > 0 ? c.opt.block_node : kBlockNode;
   const int grid = (c.nnode + bn - 1) / bn;
 #define EQD_NODE_ARGS c.vel, c.disp, c.F, c.inv_mass, c.F9, c.v9, c.vh, c.pml_ab, c.nnode, c.n_int, \
     c.npml, c.sc.dt, c.d_nt, c.d_err, c.vel32, c.dl32, c.sc.rdampk
   if (c.fp32) {
-    const NodeArgs32 a = node_args32(c);
+    NodeArgs32 a = node_args32(c);
+    a.skip_split = skip_split ? 1 : 0;
     if (c.f_is_acc) {
       if (a.damp) node_update32<true, true><<<grid, bn, 0, s>>>(a);
       else node_update32<true, false><<<grid, bn, 0, s>>>(a);
@@ -824,13 +835,14 @@ struct OutputArgs {
 // output_gm + output_src_evol (src/library_output.f90:267-312) of step nt when
 // (nt - 1) % every == 0 (src/driver.f90:30: mod(nt, 10) == 1): frame (nt - 1) / every of the ring
 // gets the velocity of every surface node and fric(47) of every pair.
-__global__ void __launch_bounds__(256) output_capture_kernel(OutputArgs o) {
+// part 1: the surface velocities, part 2: fric(47), 3: both
+__global__ void __launch_bounds__(256) output_capture_kernel(OutputArgs o, int part) {
   const int nt = *o.d_nt;
   if (nt < 1 || (nt - 1) % o.every != 0) return;
   const int f = (nt - 1) / o.every;
   const size_t len = 3 * (size_t)o.nsurf + o.npair;
   double *fr = o.frames + (size_t)(f % o.ring) * len;
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x + ((part & 1) ? 0 : o.nsurf);
   if (t < o.nsurf) {
     const int d = o.surf[t];
 #pragma unroll
@@ -843,23 +855,92 @@ __global__ void __launch_bounds__(256) output_capture_kernel(OutputArgs o) {
 }
 }  // namespace
 
-int launch_output_capture(Context &c, cudaStream_t s) {
+int launch_output_capture(Context &c, cudaStream_t s, int part, bool overlapped) {
   if (!c.out_frames) return EQD_OK;
-  const OutputArgs o{c.vel, c.fric, c.out_surf, c.d_nt, c.out_frames, c.out_count,
-                     c.nnode, c.npair, c.out_nsurf, c.out_every, c.out_ring};
-  const int n = c.out_nsurf + c.npair;
-  if (n > 0) output_capture_kernel<<<(n + 255) / 256, 256, 0, s>>>(o);
+  // the fault-side part of the overlapped schedule runs beside the next step's node update
+  const OutputArgs o{c.vel, c.fric, c.out_surf, (overlapped && part == 2) ? c.d_nt_c : c.d_nt, c.out_frames,
+                     c.out_count, c.nnode, c.npair, c.out_nsurf, c.out_every, c.out_ring};
+  const int n = ((part & 1) ? c.out_nsurf : 0) + ((part & 2) ? c.npair : 0);
+  if (n > 0) output_capture_kernel<<<(n + 255) / 256, 256, 0, s>>>(o, part);
   return cudaGetLastError() == cudaSuccess ? EQD_OK : EQD_ERR_CUDA;
 }
 
-int launch_fault(Context &c, cudaStream_t s) {
-  const int nthreads = c.npair + (c.nOffRows > 0 ? c.nOffRows + 1 : 0);
-  if (nthreads == 0) return EQD_OK;
+namespace {
+// Split nodes of the overlapped schedule (after the fault kernel of the previous step and the bulk
+// node update of this one): slot q of Fsplit is the slave (even q) or master (odd q) of pair q / 2.
+// Thread 0 also publishes the step number to d_nt_c for the fault phase of this step.
+template <bool F_IS_ACC>
+__global__ void __launch_bounds__(256) split_update32(NodeArgs32 a, const int *__restrict__ pair_s,
+                                                     const int *__restrict__ pair_m, int npair, int *d_nt_c) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q == 0) *d_nt_c = *a.d_nt;
+  if (q >= 2 * npair) return;
+  split_node_update<F_IS_ACC>(a, (q & 1) ? pair_m[q >> 1] : pair_s[q >> 1], q);
+}
+
+// Off-fault station rows (storeOffFaultStData, src/driver.f90:157-180) of the overlapped schedule:
+// taken after every node of the step is updated, before the element kernels.
+__global__ void __launch_bounds__(128) station_capture_kernel(FaultArgs p) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nt = *p.d_nt;
+  if (r > p.nOffRows || nt < 1 || nt > p.nstep || !p.offhist) return;
+  double val = p.d_times[nt];
+  if (r > 0) {
+    const int node = p.off_rows[r - 1], comp = p.off_rows[p.nOffRows + r - 1];
+    const int type = p.off_rows[2 * p.nOffRows + r - 1];
+    val = (type == 1) ? p.disp[comp * p.nnode + node] : p.vel[comp * p.nnode + node];
+  }
+  p.offhist[(size_t)(p.nOffRows + 1) * (nt - 1) + r] = val;
+}
+}  // namespace
+
+int launch_split_update(Context &c, cudaStream_t s) {
+  const NodeArgs32 a = node_args32(c);
+  const int n = std::max(2 * c.npair, 1);
+  if (c.f_is_acc) split_update32<true><<<(n + 255) / 256, 256, 0, s>>>(a, c.pair_s, c.pair_m, c.npair, c.d_nt_c);
+  else split_update32<false><<<(n + 255) / 256, 256, 0, s>>>(a, c.pair_s, c.pair_m, c.npair, c.d_nt_c);
+  return cudaGetLastError() == cudaSuccess ? EQD_OK : EQD_ERR_CUDA;
+}
+
+int launch_station_capture(Context &c, cudaStream_t s) {
+  if (c.nOffRows <= 0 || !c.offhist) return EQD_OK;
   const FaultArgs p = fault_args(c);
+  station_capture_kernel<<<(c.nOffRows + 1 + 127) / 128, 128, 0, s>>>(p);
+  return cudaGetLastError() == cudaSuccess ? EQD_OK : EQD_ERR_CUDA;
+}
+
+int launch_fault(Context &c, cudaStream_t s, bool overlapped) {
+  // overlapped schedule: the off-fault station rows are taken by station_capture_kernel, and the
+  // step number comes from d_nt_c (the bulk node update of the next step may already count it)
+  const int nthreads = c.npair + (!overlapped && c.nOffRows > 0 ? c.nOffRows + 1 : 0);
+  if (nthreads == 0) return EQD_OK;
+  FaultArgs p = fault_args(c);
+  if (overlapped) {
+    p.d_nt = c.d_nt_c;
+    p.offhist = nullptr;  // the last block's spare threads must not take station rows either
+  }
   if (p.friclaw == 5 && p.tp_hist)
     thermop_kernel<<<(c.npair + 31) / 32, 32 * kTpWarps, 0, s>>>(p);
   const int bf = c.opt.block_fault > 0 ? c.opt.block_fault : kBlockFault;
   const int grid = (nthreads + bf - 1) / bf;
+  if (overlapped) {
+    // beside the PML pass: the launch carries the highest priority itself, so that a captured
+    // graph node keeps it (a graph does not take the priority of the capturing stream)
+    int lo = 0, hi = 0;
+    cudaDeviceGetStreamPriorityRange(&lo, &hi);
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributePriority;
+    attr[0].val.priority = hi;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(bf);
+    cfg.stream = s;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    const cudaError_t e = c.fp32 ? cudaLaunchKernelEx(&cfg, fault_kernel<true>, p)
+                                 : cudaLaunchKernelEx(&cfg, fault_kernel<false>, p);
+    return e == cudaSuccess ? EQD_OK : EQD_ERR_CUDA;
+  }
   if (c.fp32) fault_kernel<true><<<grid, bf, 0, s>>>(p);
   else fault_kernel<false><<<grid, bf, 0, s>>>(p);
   return cudaGetLastError() == cudaSuccess ? EQD_OK : EQD_ERR_CUDA;

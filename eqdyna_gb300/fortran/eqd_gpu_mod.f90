@@ -33,7 +33,7 @@ module eqd_gpu_mod
 
   type, bind(C) :: eqd_options
     integer(c_int32_t) :: precision, learned_guess, record_tp_hist, tile_shape
-    integer(c_int32_t) :: use_graph, device, table_layout, block_node, block_fault, reserved
+    integer(c_int32_t) :: use_graph, device, table_layout, block_node, block_fault, sequential_fault
   end type
 
   interface

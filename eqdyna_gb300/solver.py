@@ -19,7 +19,8 @@ PRECISIONS = {"fp64": N.PREC_FP64, "fp32": N.PREC_FP32}
 
 class GpuSolver:
     def __init__(self, case, precision="fp64", learned_guess=False, use_graph=True, device=0,
-                 record_tp_hist=False, table_layout="auto", tile_shape=0, block_node=0, block_fault=0):
+                 record_tp_hist=False, table_layout="auto", tile_shape=0, block_node=0, block_fault=0,
+                 sequential_fault=False):
         self.lib = N.gpu_lib()
         self.case = case
         self._ha = case.host_arrays()
@@ -33,6 +34,7 @@ class GpuSolver:
         opt.tile_shape = int(tile_shape)
         opt.block_node = int(block_node)
         opt.block_fault = int(block_fault)
+        opt.sequential_fault = int(bool(sequential_fault))
         self._opt = opt
         h = C.c_void_p()
         rc = self.lib.eqd_gpu_init(C.byref(case.scalars), C.byref(self._ha), C.byref(opt), C.byref(h))
@@ -111,10 +113,12 @@ class GpuSolver:
         return dict(zip(["newton_iters", "newton_maxhits", "elem_updates", "kernel_launches"],
                         [v.value for v in vals]))
 
-    def profile(self, enable=True, reset=False):
+    def profile(self, enable=True, reset=False, calls_only=False):
+        """Per-launch CUDA events (the reference's order, no graph), or with calls_only events around
+        each step call only (the production path: graphs and the overlapped schedule)."""
         if reset:
             self.lib.eqd_gpu_profile(self._h, 2)
-        self.lib.eqd_gpu_profile(self._h, 1 if enable else 0)
+        self._rc(self.lib.eqd_gpu_profile(self._h, (3 if calls_only else 1) if enable else 0), "eqd_gpu_profile")
 
     KERNEL_KINDS = {"step": 0, "node_update": 1, "elem_interior": 2, "elem_pml": 3, "fault": 4}
 

@@ -136,7 +136,10 @@ typedef struct eqd_options {
   int32_t table_layout;   /* enum eqd_table_layout (binary32 form only)                        */
   int32_t block_node;     /* node-update block size: 64, 128, 256 or 512; 0 = 256                */
   int32_t block_fault;    /* fault-kernel block size: 32, 64 or 128; 0 = 128                     */
-  int32_t reserved;
+  int32_t sequential_fault; /* binary32 form: 1 runs the fault phase of a step before the next
+                             step's node update, in the reference's order; 0 (default) runs it
+                             beside the next step's bulk node update (only the update of the split
+                             nodes waits for it), with the same results                          */
 } eqd_options;
 
 typedef struct eqd_context eqd_context;
@@ -216,7 +219,9 @@ double eqd_gpu_time(eqd_context *ctx);
 
 /* Timing of subsequent eqd_gpu_step calls: with enable = 1 every step records CUDA events on
  * the library's stream around each kernel launch (the step loop is issued as plain stream
- * launches, no graph, while enabled).  enable = 0 stops and enable = 2 resets the totals. */
+ * launches in the reference's order, no graph, no overlap, while enabled); with enable = 3 only
+ * the whole call is bracketed by events (graphs and the overlapped schedule kept; kind 0 below
+ * then counts steps).  enable = 0 stops and enable = 2 resets the totals. */
 int eqd_gpu_profile(eqd_context *ctx, int32_t enable);
 
 /* Milliseconds and launch count accumulated while profiling, per kind:

@@ -126,3 +126,35 @@ def test_integer_pipe_conversions_match_hardware():
     mm = (C.c_int64 * 2)()
     assert N.gpu_lib().eqd_gpu_check_conversions(0, 1 << 24, 20261204, mm) == 0
     assert list(mm) == [0, 0]
+
+
+@pytest.mark.parametrize("name,nsteps", [("tpv8", 60), ("tpv104", 80)])
+def test_overlapped_fault_phase_matches_reference_order(name, nsteps):
+    """The default schedule runs the fault phase of step n beside the bulk node update of step
+    n + 1; the reference's order runs them one after the other.  Both must give the same state
+    (binary32 sums end in L2 reductions, so to relative 1e-5), stations included."""
+    from eqdyna_gb300.case import Case
+    from eqdyna_gb300.solver import GpuSolver
+    case = Case.from_fixture(golden_path(name))
+    runs = []
+    for seq in (False, True):
+        g = case.clone()
+        with GpuSolver(g, precision="fp32", sequential_fault=seq) as s:
+            s.step(1)
+            s.step(nsteps - 1)   # graphs of 16 steps and single steps
+            s.fetch()
+        runs.append(g)
+    a, b = runs
+
+    def rel(x, y):
+        return np.linalg.norm(x - y) / max(np.linalg.norm(y), 1e-300)
+    fa, fb = a.fric(), b.fric()
+    rep = {"slip": rel(fa[:, 70:73], fb[:, 70:73]), "slip_rate": rel(fa[:, 73:76], fb[:, 73:76]),
+           "vel": rel(a.arrays["velArr"], b.arrays["velArr"]), "disp": rel(a.arrays["dispArr"], b.arrays["dispArr"])}
+    for k in ("onFaultQuantHistSCECForm", "OffFaultStGramSCEC"):
+        if a.arrays.get(k) is not None and a.arrays[k].size:
+            rep[k] = rel(a.arrays[k], b.arrays[k])
+    print(name, rep)
+    assert all(v <= 1e-5 for v in rep.values()), rep
+    ta, tb = a.arrays["fnft"][: a.npair], b.arrays["fnft"][: b.npair]
+    assert np.array_equal(ta < 1e4, tb < 1e4)
