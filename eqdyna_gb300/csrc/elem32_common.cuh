@@ -120,18 +120,27 @@ struct TileSmem {
   unsigned short *sincp;    // [Mmax + 1] first incidence of each tile node
   int *sids;                // [Mmax] global node ids, or null (read again from the tile list)
 };
-__device__ __forceinline__ TileSmem tile_smem(float *rows_end, int Mmax, bool ids) {
+// slot_over: where slot_of lives when it overlays rows of the tile (null: its own 2 KB)
+__device__ __forceinline__ TileSmem tile_smem(float *rows_end, int Mmax, bool ids,
+                                              unsigned short *slot_over = nullptr) {
   TileSmem t;
   t.sinc = reinterpret_cast<unsigned short *>(rows_end);
-  t.slot_of = t.sinc + 8 * kTile;
-  t.sv = reinterpret_cast<float *>(t.slot_of + 8 * kTile);
+  t.slot_of = slot_over ? slot_over : t.sinc + 8 * kTile;
+  t.sv = reinterpret_cast<float *>(t.sinc + (slot_over ? 8 : 16) * kTile);
   t.sd = t.sv + 3 * Mmax;
   t.sids = ids ? reinterpret_cast<int *>(t.sd + 3 * Mmax) : nullptr;
   t.sincp = reinterpret_cast<unsigned short *>(t.sd + 3 * Mmax + (ids ? Mmax : 0));
   return t;
 }
-inline size_t tile_smem_bytes(int Mmax, bool ids) {
-  return 2 * (8 * kTile * 2) + 6 * (size_t)Mmax * 4 + (ids ? 4 * (size_t)Mmax : 0) + (((size_t)Mmax + 2) & ~(size_t)1) * 2;
+inline size_t tile_smem_bytes(int Mmax, bool ids, bool slot_over = false) {
+  return (slot_over ? 1 : 2) * (8 * kTile * 2) + 6 * (size_t)Mmax * 4 + (ids ? 4 * (size_t)Mmax : 0) +
+         (((size_t)Mmax + 2) & ~(size_t)1) * 2;
+}
+
+// The local node of each corner of this thread's element (garbage for an empty slot, unused).
+__device__ __forceinline__ void load_slots(const unsigned short *slot_of, int tid, int (&sl)[8]) {
+#pragma unroll
+  for (int a = 0; a < 8; ++a) sl[a] = slot_of[a * kTile + tid];
 }
 
 // Stages tile t: the binary32 node data, the incidence pointers and (optionally) the node ids
@@ -174,7 +183,7 @@ __device__ __forceinline__ void build_slots(const unsigned short *incp, int M, c
 // the element's constants S.q(0..4) = exp(-dt / tau_k), mu c_s, (lambda + 2 mu) c_v, 8 w_kp, 8 w_ks.
 template <bool BODY, bool PLASTIC, int HG, bool QM, class Src>
 __device__ __forceinline__ void interior_element(const Src &S, const float *sv, const float *sd, int Mmax,
-                                                 const unsigned short *slot_of, int tid,
+                                                 const int (&sl_in)[8], int tid,
                                                  const ElemConst32 &k, double *pstrain_e,
                                                  float *stress_e, size_t ld, float *fs) {
   using C = TabCommon<HG>;
@@ -186,7 +195,7 @@ __device__ __forceinline__ void interior_element(const Src &S, const float *sv, 
   int sl[8];
 #pragma unroll
   for (int a = 0; a < 8; ++a) {
-    sl[a] = slot_of[a * kTile + tid];
+    sl[a] = sl_in[a];
     const float bx = S.g(C::SHP + 3 * a), by = S.g(C::SHP + 3 * a + 1), bz = S.g(C::SHP + 3 * a + 2);
     const float vx = sv[sl[a]], vy = sv[Mmax + sl[a]], vz = sv[2 * Mmax + sl[a]];
     sr[0] = fmaf(bx, vx, sr[0]);
@@ -345,7 +354,7 @@ __device__ __forceinline__ void interior_gather(const ElemGroup<float> &g, int M
 // stress rows of S (read first), cfh the hourglass-vector rows (as fs above).
 template <bool BODY, bool S0, int HG, class Src>
 __device__ __forceinline__ void pml_element(const Src &S, const float *sv, const float *sd, int Mmax,
-                                            const unsigned short *slot_of, int tid, const ElemConst32 &k,
+                                            const int (&sl_in)[8], int tid, const ElemConst32 &k,
                                             float *stress_e, size_t ld, float *es, float *cfh) {
   using C = TabCommon<HG>;
   float D[3][3];
@@ -357,7 +366,7 @@ __device__ __forceinline__ void pml_element(const Src &S, const float *sv, const
   int sl[8];
 #pragma unroll
   for (int a = 0; a < 8; ++a) {
-    sl[a] = slot_of[a * kTile + tid];
+    sl[a] = sl_in[a];
     const float b[3] = {S.g(C::SHP + 3 * a), S.g(C::SHP + 3 * a + 1), S.g(C::SHP + 3 * a + 2)};
     const float v[3] = {sv[sl[a]], sv[Mmax + sl[a]], sv[2 * Mmax + sl[a]]};
 #pragma unroll

@@ -55,8 +55,30 @@ int dalloc(Context &c, T *&p, size_t n) {
   return EQD_OK;
 }
 
-template <typename T>
-int dupload(Context &c, T *&p, const std::vector<T> &h) {
+// Allocator whose vectors leave new elements uninitialised: the element setup writes every entry
+// of its scratch tables (tens of GB on C1-size meshes) once, in parallel, so a zero-fill in the
+// constructor would only double the host memory traffic (single-threaded).
+template <class T>
+struct NoInitAlloc : std::allocator<T> {
+  template <class U>
+  struct rebind {
+    using other = NoInitAlloc<U>;
+  };
+  NoInitAlloc() = default;
+  template <class U>
+  NoInitAlloc(const NoInitAlloc<U> &) noexcept {}
+  template <class U>
+  void construct(U *) noexcept {}
+  template <class U, class... Args>
+  void construct(U *p, Args &&...args) {
+    ::new ((void *)p) U(std::forward<Args>(args)...);
+  }
+};
+template <class T>
+using Scratch = std::vector<T, NoInitAlloc<T>>;
+
+template <typename T, class A>
+int dupload(Context &c, T *&p, const std::vector<T, A> &h) {
   int rc = dalloc(c, p, h.size());
   if (rc) return rc;
   if (!h.empty() && cudaMemcpy(p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice) != cudaSuccess)
@@ -186,7 +208,7 @@ void brick_order(const eqd_host_arrays &a, std::vector<int> &ids, int bx, int bz
 // Tile metadata: per tile its distinct nodes and, per node, the incidences (corner * tile + local
 // element) in ascending order.  Nodes are ordered by incidence count (most first), then by device
 // id, so the 32 nodes of a warp in the gather loop have (nearly) the same trip count.
-int build_tiles(Context &c, ElemGroup<float> &g, const std::vector<int> &conn_dev, int tile) {
+int build_tiles(Context &c, ElemGroup<float> &g, const Scratch<int> &conn_dev, int tile) {
   const int m = g.ne;
   g.tile = tile;
   g.ntiles = (m + tile - 1) / tile;
@@ -320,7 +342,8 @@ class RecordDict {
 constexpr long kAutoMaxRecords = 65536;
 
 // binary32 copy of a component-major table [ncomp][m] with its rows padded with zeros to stride ld
-std::vector<float> to_f32_rows(const std::vector<double> &v, size_t m, size_t ld) {
+template <class V>
+std::vector<float> to_f32_rows(const V &v, size_t m, size_t ld) {
   const size_t nc = v.size() / m;
   std::vector<float> out(nc * ld, 0.f);
 #pragma omp parallel for schedule(static)
@@ -381,7 +404,8 @@ int build_device_state(eqd_context &X, const eqd_scalars &s, const eqd_host_arra
   }
   c.npml = nn - c.n_int;
   const int np_ = c.npml;
-  std::vector<double> vel(3 * (size_t)nn), disp(3 * (size_t)nn), F(3 * (size_t)nn, 0.0), inv_mass(nn, 0.0);
+  Scratch<double> vel(3 * (size_t)nn), disp(3 * (size_t)nn);  // every entry written below
+  std::vector<double> F(3 * (size_t)nn, 0.0), inv_mass(nn, 0.0);
   std::vector<double> F9(9 * (size_t)np_, 0.0), v9(9 * (size_t)np_, 0.0), vh(3 * (size_t)np_, 0.0);
   std::vector<double> pml_ab(6 * (size_t)np_, 0.0);
   int bad_ = EQD_OK;
@@ -509,10 +533,11 @@ int build_device_state(eqd_context &X, const eqd_scalars &s, const eqd_host_arra
     if (!c.fp32) g.ne = m;
     else (grp == 0 ? c.gi32 : c.gp32).ne = m;
     if (m == 0) continue;
-    std::vector<int> conn(8 * (size_t)m);
-    std::vector<double> shp(24 * (size_t)m), phi(32 * (size_t)m), ss(6 * (size_t)m), detw(m), lam(m), mu(m);
+    Scratch<int> conn(8 * (size_t)m);
+    Scratch<double> shp(24 * (size_t)m), phi(32 * (size_t)m), ss(6 * (size_t)m), detw(m), lam(m), mu(m);
     const int nstress = grp == 0 ? (s.C_Q != 0 ? 12 : 6) : 15;
-    std::vector<double> st(nstress * (size_t)m), st0, pab, em, hg, porep, pstr, qc;
+    Scratch<double> st(nstress * (size_t)m);
+    std::vector<double> st0, pab, em, hg, porep, pstr, qc;
     bool any_s0 = false;
     int s0_any = 0;
     if (grp == 1) st0.assign(6 * (size_t)m, 0.0), pab.assign(6 * (size_t)m, 0.0);
@@ -527,6 +552,11 @@ int build_device_state(eqd_context &X, const eqd_scalars &s, const eqd_host_arra
         const int e = ids[i];
         if (e < 0) {  // empty slot of the binary32 tiles: no nodes, zero tables
           for (int q = 0; q < 8; ++q) conn[q * (size_t)m + i] = -1;
+          for (int q = 0; q < 24; ++q) shp[q * (size_t)m + i] = 0.0;
+          for (int q = 0; q < 32; ++q) phi[q * (size_t)m + i] = 0.0;
+          for (int q = 0; q < 6; ++q) ss[q * (size_t)m + i] = 0.0;
+          for (int q = 0; q < nstress; ++q) st[q * (size_t)m + i] = 0.0;
+          detw[i] = lam[i] = mu[i] = 0.0;
           return EQD_OK;
         }
         double ctr[3] = {0, 0, 0};
@@ -1379,12 +1409,12 @@ int eqd_gpu_fetch(eqd_context *X, eqd_host_arrays *a) {
   EQD_CUDA_OK(cudaStreamSynchronize(c.stream));
   if (a->nnode != c.nnode || a->nelem != c.nelem) return EQD_ERR_INPUT;
   const int nn = c.nnode, np_ = c.npml;
-  std::vector<double> vel(3 * (size_t)nn), disp(3 * (size_t)nn), F(3 * (size_t)nn), im(nn);
+  Scratch<double> vel(3 * (size_t)nn), disp(3 * (size_t)nn), F(3 * (size_t)nn), im(nn);  // copied into
   std::vector<double> v9(9 * (size_t)np_), vh(3 * (size_t)np_), F9(9 * (size_t)np_);
   EQD_CUDA_OK(cudaMemcpy(vel.data(), c.vel, vel.size() * 8, cudaMemcpyDeviceToHost));
   EQD_CUDA_OK(cudaMemcpy(disp.data(), c.disp, disp.size() * 8, cudaMemcpyDeviceToHost));
   EQD_CUDA_OK(cudaMemcpy(im.data(), c.inv_mass, im.size() * 8, cudaMemcpyDeviceToHost));
-  auto get32 = [&](std::vector<double> &dst, const float *src) -> int {
+  auto get32 = [&](auto &dst, const float *src) -> int {
     std::vector<float> t(dst.size());
     if (!t.empty() && cudaMemcpy(t.data(), src, t.size() * 4, cudaMemcpyDeviceToHost) != cudaSuccess) return EQD_ERR_CUDA;
     const long long nt = (long long)t.size();

@@ -110,8 +110,10 @@ __global__ void __launch_bounds__(kTile)
   __syncthreads();
   const int e = e0 + tid;
   float *fs = tab + L::FS * kTile;
+  int sl[8];
+  load_slots(slot_of, tid, sl);
   if (tid < live)
-    interior_element<BODY, PLASTIC, HG, false>(SlabSrc<L>{tab, tid}, sv, sd, Mmax, slot_of, tid, k,
+    interior_element<BODY, PLASTIC, HG, false>(SlabSrc<L>{tab, tid}, sv, sd, Mmax, sl, tid, k,
                                         PLASTIC ? g.pstrain + e : nullptr, g.stress + e, (size_t)ld, fs);
   __syncthreads();
   interior_gather(g, M, nb, incp, sinc, fs, F, nnode, ts.sids);
@@ -155,8 +157,10 @@ __global__ void __launch_bounds__(kTile)
   const int e = e0 + tid;
   float *cfh = tab + L::FS * kTile;
   float *es = tab + L::ES * kTile;
+  int sl[8];
+  load_slots(slot_of, tid, sl);
   if (tid < live)
-    pml_element<BODY, S0, HG>(SlabSrc<L>{tab, tid}, sv, sd, Mmax, slot_of, tid, k, g.stress + e, (size_t)ld,
+    pml_element<BODY, S0, HG>(SlabSrc<L>{tab, tid}, sv, sd, Mmax, sl, tid, k, g.stress + e, (size_t)ld,
                               es, cfh);
   __syncthreads();
   auto src_of = [&](int el) { return SlabSrc<L>{tab, el}; };

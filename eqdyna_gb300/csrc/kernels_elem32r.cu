@@ -18,6 +18,7 @@
 // into shared memory while all threads gather the tile's node data; then the element math and the
 // node gather of elem32_common.cuh.
 #include <algorithm>
+#include <type_traits>
 #include <vector>
 
 #include "elem32_common.cuh"
@@ -44,6 +45,10 @@ struct RecInterior {
   static constexpr int FS = 0;                           // 24 rows of per-corner forces (overlay)
   static constexpr int NS = 24;
   static constexpr bool IDS = false;                     // node ids re-read by the gather
+  // the slot table (2 KB) overlays force rows 20-23 (written last, after a barrier that follows
+  // the reads of every slot): 10 CTAs per SM instead of 9 on C1
+  static constexpr int SLOT = 20;
+  static_assert(N <= SLOT, "slot rows clear of the copied rows");
 };
 template <bool BODY, bool S0, int HG>
 struct RecPml {
@@ -57,7 +62,8 @@ struct RecPml {
   static constexpr int ES = STR;                         // 6 split-stress sums over the stress rows
   static constexpr int FS = ES + 6;                      // 24 rows of per-corner forces (overlay)
   static constexpr int NS = FS + 24;
-  static constexpr bool IDS = true;                      // node ids staged in shared memory
+  static constexpr bool IDS = false;                     // node ids re-read by the gather: staging
+                                                         // them costs the 8th CTA per SM
   static_assert(NS >= N, "copied rows fit");
 };
 
@@ -128,7 +134,8 @@ __device__ __forceinline__ void interior_rec_body(const ElemArgs32 &a, int tile)
   const ElemGroup<float> &g = a.g;
   const int Mmax = g.max_tile_nodes;
   float *tab = reinterpret_cast<float *>(smem);
-  const TileSmem ts = tile_smem(tab + L::NS * kTile, Mmax, L::IDS);
+  const TileSmem ts = tile_smem(tab + L::NS * kTile, Mmax, L::IDS,
+                                reinterpret_cast<unsigned short *>(tab + L::SLOT * kTile));
   unsigned short *sinc = ts.sinc, *slot_of = ts.slot_of;
   float *sv = ts.sv, *sd = ts.sd;
   const int tid = threadIdx.x;
@@ -153,14 +160,17 @@ __device__ __forceinline__ void interior_rec_body(const ElemArgs32 &a, int tile)
   __syncthreads();
   const int e = e0 + tid;
   float *fs = tab + L::FS * kTile;
+  int sl[8];
+  load_slots(slot_of, tid, sl);
+  __syncthreads();  // every slot read before the force rows over the slot table are written
   if (tid < live) {
     double *ps = PLASTIC ? g.pstrain + e : nullptr;
     if (UNI) {
       const UniSrc<L> S{a.rp, tab, tid, nullptr, 0, 0u, 0u};
-      interior_element<BODY, PLASTIC, HG, QM>(S, sv, sd, Mmax, slot_of, tid, a.k, ps, g.stress + e, (size_t)ld, fs);
+      interior_element<BODY, PLASTIC, HG, QM>(S, sv, sd, Mmax, sl, tid, a.k, ps, g.stress + e, (size_t)ld, fs);
     } else {
       const RecSrc<L> S{g.rec + (size_t)row_u32(tab, L::RID, tid) * g.rec_len, tab, tid, nullptr, 0, 0u, 0u};
-      interior_element<BODY, PLASTIC, HG, QM>(S, sv, sd, Mmax, slot_of, tid, a.k, ps, g.stress + e, (size_t)ld, fs);
+      interior_element<BODY, PLASTIC, HG, QM>(S, sv, sd, Mmax, sl, tid, a.k, ps, g.stress + e, (size_t)ld, fs);
     }
   }
   __syncthreads();
@@ -207,15 +217,17 @@ __device__ __forceinline__ void pml_rec_body(const ElemArgs32 &a, int tile) {
   float *es = tab + L::ES * kTile;
   const float *rec = g.rec;
   const int rlen = g.rec_len;
+  int sl[8];
+  load_slots(slot_of, tid, sl);
   if (tid < live) {
     const unsigned ab01 = row_u32(tab, L::ABID, tid), ab2 = row_u32(tab, L::ABID + 1, tid);
     if (UNI) {
       const UniSrc<L> S{a.rp, tab, tid, g.ab_tab, g.ab_stride, ab01, ab2};
-      pml_element<BODY, S0, HG>(S, sv, sd, Mmax, slot_of, tid, a.k, g.stress + e, (size_t)ld, es, cfh);
+      pml_element<BODY, S0, HG>(S, sv, sd, Mmax, sl, tid, a.k, g.stress + e, (size_t)ld, es, cfh);
     } else {
       const RecSrc<L> S{rec + (size_t)row_u32(tab, L::RID, tid) * rlen, tab, tid, g.ab_tab, g.ab_stride,
                         ab01, ab2};
-      pml_element<BODY, S0, HG>(S, sv, sd, Mmax, slot_of, tid, a.k, g.stress + e, (size_t)ld, es, cfh);
+      pml_element<BODY, S0, HG>(S, sv, sd, Mmax, sl, tid, a.k, g.stress + e, (size_t)ld, es, cfh);
     }
   }
   __syncthreads();
@@ -283,9 +295,14 @@ __global__ void __launch_bounds__(kTile) elem_pml_rec_batched(const ElemArgs32 *
   else pml_rec_body<BODY, S0, HG, false>(a, tile);
 }
 
+template <class L, class = void>
+struct SlotOver : std::false_type {};
+template <class L>
+struct SlotOver<L, std::void_t<decltype(L::SLOT)>> : std::true_type {};
+
 template <class L>
 size_t rec_smem(int Mmax) {
-  return (size_t)L::NS * kTile * 4 + tile_smem_bytes(Mmax, L::IDS);
+  return (size_t)L::NS * kTile * 4 + tile_smem_bytes(Mmax, L::IDS, SlotOver<L>::value);
 }
 
 ElemArgs32 elem_args(const Context &c, bool interior, const ElemConst32 &k) {
