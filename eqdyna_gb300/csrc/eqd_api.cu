@@ -146,9 +146,9 @@ void q_constants(double Q, int k, double &tau, double &wk, double &c1) {
 // tile (at a mesh edge) is followed by empty slots (-1) up to the tile boundary, so that every tile
 // holds one brick: without them one partial brick shifts every later tile across two bricks
 // (C1 at dx = 200 m: 262 instead of 214 distinct nodes per tile on average, 311 at most).
-void brick_order(const eqd_host_arrays &a, std::vector<int> &ids, int bx, int bz, int by, int tile) {
+bool brick_order(const eqd_host_arrays &a, std::vector<int> &ids, int bx, int bz, int by, int tile) {
   const size_t m = ids.size();
-  if (m == 0) return;
+  if (m == 0) return true;
   std::vector<double> c(3 * m), ext(3 * m);
   double lo0 = 1e300, lo1 = 1e300, lo2 = 1e300;
 #pragma omp parallel for schedule(static) reduction(min : lo0, lo1, lo2)
@@ -178,31 +178,36 @@ void brick_order(const eqd_host_arrays &a, std::vector<int> &ids, int bx, int bz
     std::nth_element(e.begin(), e.begin() + m / 2, e.end());
     h[k] = e[m / 2] > 0 ? e[m / 2] : 1.0;
   }
-  using Key = std::tuple<long, long, long, long, long, long, int>;
-  std::vector<Key> keys(m);
-#pragma omp parallel for schedule(static)
+  // sort key (brick x, brick z, brick y, then x, z, y inside the brick, then the element), packed
+  // into 64 bits: 16 bits per brick index, 16 for the position inside the brick
+  std::vector<std::pair<uint64_t, int>> keys(m);
+  int wide = 0;
+#pragma omp parallel for schedule(static) reduction(| : wide)
   for (size_t i = 0; i < m; ++i) {
     const long fx = (long)std::floor((c[3 * i] - lo[0]) / h[0] + 0.5);
     const long fy = (long)std::floor((c[3 * i + 1] - lo[1]) / h[1] + 0.5);
     const long fz = (long)std::floor((c[3 * i + 2] - lo[2]) / h[2] + 0.5);
-    keys[i] = Key(fx / bx, fz / bz, fy / by, fx, fz, fy, ids[i]);
+    const uint64_t b0 = (uint64_t)(fx / bx), b1 = (uint64_t)(fz / bz), b2 = (uint64_t)(fy / by);
+    const uint64_t w = (uint64_t)(fx % bx) << 11 | (uint64_t)(fz % bz) << 6 | (uint64_t)(fy % by);
+    if (fx < 0 || fy < 0 || fz < 0 || b0 > 0xffff || b1 > 0xffff || b2 > 0xffff) wide = 1;
+    keys[i] = {b0 << 48 | b1 << 32 | b2 << 16 | w, ids[i]};
   }
+  if (wide || bx > 32 || bz > 32 || by > 64) return false;  // not representable: caller falls back
   __gnu_parallel::sort(keys.begin(), keys.end());
   if (bx * by * bz != tile) {
 #pragma omp parallel for schedule(static)
-    for (size_t i = 0; i < m; ++i) ids[i] = std::get<6>(keys[i]);
-    return;
+    for (size_t i = 0; i < m; ++i) ids[i] = keys[i].second;
+    return true;
   }
   ids.clear();
   ids.reserve(m + m / 8);
   for (size_t i = 0; i < m; ++i) {
-    const bool new_brick = i > 0 && (std::get<0>(keys[i]) != std::get<0>(keys[i - 1]) ||
-                                     std::get<1>(keys[i]) != std::get<1>(keys[i - 1]) ||
-                                     std::get<2>(keys[i]) != std::get<2>(keys[i - 1]));
+    const bool new_brick = i > 0 && (keys[i].first >> 16) != (keys[i - 1].first >> 16);
     if (new_brick)
       while (ids.size() % tile) ids.push_back(-1);
-    ids.push_back(std::get<6>(keys[i]));
+    ids.push_back(keys[i].second);
   }
+  return true;
 }
 
 // Tile metadata: per tile its distinct nodes and, per node, the incidences (corner * tile + local
@@ -522,6 +527,7 @@ int build_device_state(eqd_context &X, const eqd_scalars &s, const eqd_host_arra
     if (s.C_Q != 0 && c.opt.table_layout == EQD_TABLES_STREAMED) return EQD_ERR_UNSUPPORTED;
     const int ts = c.opt.tile_shape > 0 ? c.opt.tile_shape : (4 | 8 << 8 | 4 << 16);
     const int bx = ts & 255, by = (ts >> 8) & 255, bz = (ts >> 16) & 255;
+    // (a mesh wider than 65536 bricks along an axis keeps the input order)
     brick_order(a, X.gi_orig, bx, bz, by, tile_size_interior());
     brick_order(a, X.gp_orig, bx, bz, by, tile_size_pml());
   }
