@@ -717,10 +717,15 @@ int build_device_state(eqd_context &X, const eqd_scalars &s, const eqd_host_arra
       if (use_rec && grp == 1) {  // PML factors: distinct (a_k, b_k) per axis
         abid.assign(2 * ld, 0u);
         std::vector<float> pairs[3];
-        for (int k = 0; k < 3 && use_rec; ++k) {
+        std::vector<unsigned> axis_id[3];
+        int overflow_ab = 0;
+        // the three axes are independent dictionaries: one thread each
+#pragma omp parallel for schedule(static, 1) num_threads(3) reduction(| : overflow_ab)
+        for (int k = 0; k < 3; ++k) {
           std::unordered_map<uint64_t, unsigned> seen;
           uint64_t last_key = ~0ull;
           unsigned last = 0;
+          axis_id[k].assign(m, 0u);
           for (int i = 0; i < m; ++i) {
             const float fa = (float)pab[k * um + i], fb = (float)pab[(3 + k) * um + i];
             uint32_t ba, bb;
@@ -732,7 +737,7 @@ int build_device_state(eqd_context &X, const eqd_scalars &s, const eqd_host_arra
               if (it != seen.end()) {
                 last = it->second;
               } else {
-                if ((int)seen.size() >= kPmlAxisMax) { use_rec = false; break; }
+                if ((int)seen.size() >= kPmlAxisMax) { overflow_ab = 1; break; }
                 last = (unsigned)seen.size();
                 seen.emplace(key, last);
                 pairs[k].push_back(fa);
@@ -740,9 +745,15 @@ int build_device_state(eqd_context &X, const eqd_scalars &s, const eqd_host_arra
               }
               last_key = key;
             }
-            if (k == 0) abid[i] |= last;
-            else if (k == 1) abid[i] |= last << 16;
-            else abid[ld + i] = last;
+            axis_id[k][i] = last;
+          }
+        }
+        if (overflow_ab) use_rec = false;
+        if (use_rec) {
+#pragma omp parallel for schedule(static)
+          for (int i = 0; i < m; ++i) {
+            abid[i] = axis_id[0][i] | axis_id[1][i] << 16;
+            abid[ld + i] = axis_id[2][i];
           }
         }
         if (use_rec) {
