@@ -22,16 +22,14 @@ constexpr int kBlockNode = 256;       // default node-update block
 constexpr int kBlockNodeMax = 512;
 constexpr int kBlockFault = 128;      // default and largest fault-kernel block
 
-// COPY32: also writes the binary32 copies of velocity and of u + rdampk v read by the binary32
-// element kernels (the binary64 arrays stay the state).
-template <bool F_IS_ACC, bool COPY32>
+// Node update of the binary64 form (velDispUpdate, src/driver.f90:89-155; comdampv for PML nodes).
+template <bool F_IS_ACC>
 __global__ void __launch_bounds__(kBlockNodeMax)
     node_update(double *__restrict__ vel, double *__restrict__ disp, double *__restrict__ F,
                 const double *__restrict__ inv_mass, double *__restrict__ F9,
                 double *__restrict__ v9, double *__restrict__ vh,
                 const double *__restrict__ pml_ab, int nnode, int n_int, int npml, double dt,
-                int *__restrict__ d_nt, int *__restrict__ d_err, float *__restrict__ vel32,
-                float *__restrict__ dl32, double rdampk) {
+                int *__restrict__ d_nt, int *__restrict__ d_err) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i == 0) *d_nt += 1;
   if (i >= nnode) return;
@@ -82,13 +80,6 @@ __global__ void __launch_bounds__(kBlockNodeMax)
         disp[c * nnode + i] = fma(v[c], dt, disp[c * nnode + i]);
         F[c * nnode + i] = 0.0;
       }
-    }
-  }
-  if (COPY32) {
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      vel32[c * nnode + i] = (float)v[c];
-      dl32[c * nnode + i] = (float)fma(rdampk, v[c], disp[c * nnode + i]);
     }
   }
   if (isnan(v[0]) || isnan(v[1]) || isnan(v[2])) atomicOr(d_err, 1);
@@ -731,7 +722,7 @@ int launch_node_update(Context &c, cudaStream_t s, bool skip_split) {
   const int bn = c.opt.block_node > 0 ? c.opt.block_node : kBlockNode;
   const int grid = (c.nnode + bn - 1) / bn;
 #define EQD_NODE_ARGS c.vel, c.disp, c.F, c.inv_mass, c.F9, c.v9, c.vh, c.pml_ab, c.nnode, c.n_int, \
-    c.npml, c.sc.dt, c.d_nt, c.d_err, c.vel32, c.dl32, c.sc.rdampk
+    c.npml, c.sc.dt, c.d_nt, c.d_err
   if (c.fp32) {
     NodeArgs32 a = node_args32(c);
     a.skip_split = skip_split ? 1 : 0;
@@ -743,8 +734,8 @@ int launch_node_update(Context &c, cudaStream_t s, bool skip_split) {
       else node_update32<false, false><<<grid, bn, 0, s>>>(a);
     }
   } else {
-    if (c.f_is_acc) node_update<true, false><<<grid, bn, 0, s>>>(EQD_NODE_ARGS);
-    else node_update<false, false><<<grid, bn, 0, s>>>(EQD_NODE_ARGS);
+    if (c.f_is_acc) node_update<true><<<grid, bn, 0, s>>>(EQD_NODE_ARGS);
+    else node_update<false><<<grid, bn, 0, s>>>(EQD_NODE_ARGS);
   }
 #undef EQD_NODE_ARGS
   return cudaGetLastError() == cudaSuccess ? EQD_OK : EQD_ERR_CUDA;
