@@ -355,7 +355,8 @@ def bench_ours(args, world, rank, local):
     del e2e_case
 
     # ---- device-timed steps (inputs resident in HBM) ----
-    s = GpuSolver(case.clone(), precision=args.precision, learned_guess=args.learned, device=local,
+    dev_case = case.clone()
+    s = GpuSolver(dev_case, precision=args.precision, learned_guess=args.learned, device=local,
                   table_layout=args.tables, **launch)
     if args.learned:
         s.set_mlp(params, norm)
@@ -386,7 +387,36 @@ def bench_ours(args, world, rank, local):
     dev_s = allreduce_max(timed_ms / 1e3, world)
     units = allreduce_sum(float(ne) * args.steps, world)
     value = units / dev_s
+    total_steps_run = args.warmup + min(args.steps, 40) + args.steps
+    s.fetch_fault()
     s.close()
+
+    # ---- the plain binary64 method on the same steps: its speed, and the accuracy condition of
+    # the metric (slip-rate relative L2 of this run against it; the binary64 form matches the
+    # oracle to 1e-9 in tests/test_gpu_parity.py) ----
+    plain = None
+    if args.precision == "fp32" and args.plain_check:
+        ref_case = case.clone()
+        with GpuSolver(ref_case, precision="fp64", device=local) as r:
+            r.step(args.warmup + min(args.steps, 40))
+            r.profile(True, reset=True, calls_only=True)
+            r.step(args.steps)
+            r.profile(False)
+            fp64_ms = r.kernel_times()["step"][0]
+            r.fetch_fault()
+        fa, fb = dev_case.fric(), ref_case.fric()
+        scale = max(np.linalg.norm(fb[:, 73:75]), np.linalg.norm(fb[:, 75]), 1e-300)
+        fp64_value = ne * args.steps / (fp64_ms / 1e3)
+        plain = {"value": fp64_value, "ms_per_step": fp64_ms / args.steps,
+                 "speedup": value / world / fp64_value if fp64_value > 0 else None,
+                 "steps_compared": total_steps_run,
+                 "slip_rate_rel_l2": float(np.linalg.norm(fa[:, 73:75] - fb[:, 73:75]) / scale),
+                 "slip_rel_l2": float(np.linalg.norm(fa[:, 70:72] - fb[:, 70:72]) /
+                                      max(np.linalg.norm(fb[:, 70:72]), 1e-300)),
+                 "peak_rate_rel_l2": float(np.linalg.norm(fa[:, 75] - fb[:, 75]) /
+                                           max(np.linalg.norm(fb[:, 75]), 1e-300)),
+                 "note": "plain binary64 method (reference iteration, no learned guess) on this GPU over "
+                         "the same steps; errors of this run's final fault state against it"}
 
     # ---- rooflines: every kernel, the one with the largest time share on top ----
     hbm_peak, peak_kind = _peaks()
@@ -454,6 +484,7 @@ def bench_ours(args, world, rank, local):
                             "array"
                             + ("; the first steps run the plain Newton with solve logging, then training"
                                if args.learned else "")},
+            "plain_fp64": plain,
             "gpu_launches": int(stats["kernel_launches"]),
             "newton": newton,
             "learned": learned,
@@ -565,6 +596,8 @@ def main():
     ap.add_argument("--tables", default="auto", choices=["auto", "streamed", "records"],
                     help="binary32 element-table layout")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--plain-check", type=int, default=1,
+                    help="also run the plain binary64 method on the same steps (speed and accuracy)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     args = ap.parse_args()
     if args.warmup < 3:
