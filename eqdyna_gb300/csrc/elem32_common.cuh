@@ -115,7 +115,7 @@ struct TabCommon {
 // staged node data, the tile's incidence pointers and (optionally) its node ids.
 struct TileSmem {
   unsigned short *sinc;     // [8 * kTile] incidences (corner * kTile + element), node-major
-  unsigned short *slot_of;  // [8 * kTile] local node of (corner, element)
+  unsigned short *slot_of;  // [8 * kTile] local node of (corner, element), layout slot_index
   float *sv, *sd;           // [3][Mmax] binary32 velocity and u + rdampk v of the tile's nodes
   unsigned short *sincp;    // [Mmax + 1] first incidence of each tile node
   int *sids;                // [Mmax] global node ids, or null (read again from the tile list)
@@ -137,10 +137,32 @@ inline size_t tile_smem_bytes(int Mmax, bool ids, bool slot_over = false) {
          (((size_t)Mmax + 2) & ~(size_t)1) * 2;
 }
 
+// Slot table layout: the two 16-bit entries of corners 2k and 2k + 1 of element e share one 32-bit
+// word at word k * kTile + e, so that the table is four rows of kTile words whose column e belongs
+// to element e alone (it can overlay rows of per-element data).
+__host__ __device__ __forceinline__ int slot_index(int r) {  // r = corner * kTile + element
+  const int a = r / kTile, e = r - a * kTile;
+  return (a >> 1) * (2 * kTile) + 2 * e + (a & 1);
+}
+
 // The local node of each corner of this thread's element (garbage for an empty slot, unused).
 __device__ __forceinline__ void load_slots(const unsigned short *slot_of, int tid, int (&sl)[8]) {
+  const unsigned *w = reinterpret_cast<const unsigned *>(slot_of);
 #pragma unroll
-  for (int a = 0; a < 8; ++a) sl[a] = slot_of[a * kTile + tid];
+  for (int k = 0; k < 4; ++k) {
+    const unsigned v = w[k * kTile + tid];
+    sl[2 * k] = (int)(v & 0xffffu);
+    sl[2 * k + 1] = (int)(v >> 16);
+  }
+}
+
+// slot_of from the staged incidence list (node j of the tile owns incidences incp[j] .. incp[j+1]).
+__device__ __forceinline__ void build_slots(const unsigned short *incp, int M, const unsigned short *sinc,
+                                            unsigned short *slot_of) {
+  for (int j = threadIdx.x; j < M; j += blockDim.x) {
+    const int q1 = incp[j + 1];
+    for (int q = incp[j]; q < q1; ++q) slot_of[slot_index(sinc[q])] = (unsigned short)j;
+  }
 }
 
 // Stages tile t: the binary32 node data, the incidence pointers and (optionally) the node ids
@@ -163,15 +185,6 @@ __device__ __forceinline__ int stage_nodes(const ElemGroup<float> &g, int t, con
   }
   if (threadIdx.x == 0) ts.sincp[M] = incp[M];
   return M;
-}
-
-// slot_of[corner * kTile + e] = local node index, from the staged incidence list.
-__device__ __forceinline__ void build_slots(const unsigned short *incp, int M, const unsigned short *sinc,
-                                            unsigned short *slot_of) {
-  for (int j = threadIdx.x; j < M; j += blockDim.x) {
-    const int q1 = incp[j + 1];
-    for (int q = incp[j]; q < q1; ++q) slot_of[sinc[q]] = (unsigned short)j;
-  }
 }
 
 // ---- element math ------------------------------------------------------------------------------
@@ -335,6 +348,8 @@ __device__ __forceinline__ void interior_gather(const ElemGroup<float> &g, int M
                                                 const float *fs, float *__restrict__ F, int nnode,
                                                 const int *sids) {
   for (int j = threadIdx.x; j < M; j += blockDim.x) {
+    // the node id is loaded first: its latency runs under the sums
+    const int n = sids ? sids[j] : __ldg(g.tile_nodes + nb + j);
     float hi[3] = {0.f, 0.f, 0.f}, lo[3] = {0.f, 0.f, 0.f};
     const int q1 = incp[j + 1];
     for (int q = incp[j]; q < q1; ++q) {
@@ -343,7 +358,6 @@ __device__ __forceinline__ void interior_gather(const ElemGroup<float> &g, int M
 #pragma unroll
       for (int c = 0; c < 3; ++c) kahan_add(hi[c], lo[c], fs[(c * 8 + a) * kTile + el]);
     }
-    const int n = sids ? sids[j] : g.tile_nodes[nb + j];
 #pragma unroll
     for (int c = 0; c < 3; ++c) atomicAdd(F + (size_t)c * nnode + n, hi[c] - lo[c]);
   }
@@ -469,6 +483,8 @@ __device__ __forceinline__ void pml_gather(const ElemGroup<float> &g, int M, int
                                            const WOf &w_of, float *__restrict__ F, float *__restrict__ F9,
                                            int nnode, int n_int, int npml, const int *sids) {
   for (int j = threadIdx.x; j < M; j += blockDim.x) {
+    // the node id is loaded first: its latency runs under the sums
+    const int n = sids ? sids[j] : __ldg(g.tile_nodes + nb + j);
     float hi[12], lo[12];
 #pragma unroll
     for (int q = 0; q < 12; ++q) hi[q] = lo[q] = 0.f;
@@ -487,7 +503,6 @@ __device__ __forceinline__ void pml_gather(const ElemGroup<float> &g, int M, int
 #pragma unroll
       for (int c = 0; c < 3; ++c) kahan_add(hi[9 + c], lo[9 + c], cfh[(c * 8 + a) * kTile + el]);
     }
-    const int n = sids ? sids[j] : g.tile_nodes[nb + j];
     if (n >= n_int) {
       const int slot = n - n_int;
 #pragma unroll

@@ -8,6 +8,7 @@
 #include <vector>
 
 #include "eqd_device.cuh"
+#include "elem32_common.cuh"
 #include "mlp_common.cuh"
 
 #include <omp.h>
@@ -218,7 +219,7 @@ int build_tiles(Context &c, ElemGroup<float> &g, const Scratch<int> &conn_dev, i
   g.tile = tile;
   g.ntiles = (m + tile - 1) / tile;
   const int nt = g.ntiles;
-  std::vector<unsigned short> inc((size_t)nt * tile * 8, 0);
+  std::vector<unsigned short> inc((size_t)nt * tile * 8, 0), slot((size_t)nt * tile * 8, 0);
   std::vector<std::vector<int>> tnodes(nt);
   std::vector<std::vector<unsigned short>> tincp(nt);
   std::vector<int> tile_ne(nt, 0);
@@ -249,9 +250,13 @@ int build_tiles(Context &c, ElemGroup<float> &g, const Scratch<int> &conn_dev, i
     incp.reserve(runs.size() + 1);
     size_t k = 0;
     for (const auto &run : runs) {
+      const unsigned short j = (unsigned short)nodes.size();
       nodes.push_back(pairs[run.first].first);
       incp.push_back((unsigned short)k);
-      for (size_t q = run.first; q < run.second; ++q) inc[base + k++] = (unsigned short)pairs[q].second;
+      for (size_t q = run.first; q < run.second; ++q) {
+        inc[base + k++] = (unsigned short)pairs[q].second;
+        slot[base + e32::slot_index(pairs[q].second)] = j;
+      }
     }
     incp.push_back((unsigned short)pairs.size());
     maxM = std::max(maxM, (int)runs.size());
@@ -280,6 +285,7 @@ int build_tiles(Context &c, ElemGroup<float> &g, const Scratch<int> &conn_dev, i
   if ((rc = dupload(c, g.tile_incp, incp))) return rc;
   if ((rc = dupload(c, g.tile_incp_off, incp_off))) return rc;
   if ((rc = dupload(c, g.tile_inc, inc))) return rc;
+  if ((rc = dupload(c, g.tile_slot, slot))) return rc;
   return EQD_OK;
 }
 

@@ -54,6 +54,7 @@ struct ElemGroup {
   unsigned short *tile_incp = nullptr;  // per tile: M + 1 offsets into that tile's incidences
   int *tile_incp_off = nullptr;     // [ntiles + 1] offsets into tile_incp
   unsigned short *tile_inc = nullptr;   // [ntiles * tile * 8] incidences (corner * tile + e_local)
+  unsigned short *tile_slot = nullptr;  // [ntiles * tile * 8] local node of (corner, e_local)
   // record-indexed binary32 tables (nrec > 0): elements with bit-identical geometry and material
   // share one record [shp 24 | phi 32, ss 6 (or hgcoef 1) | detw, lam, mu | em 8], and the
   // per-element tables above (shp ... em, pml_ab) are not allocated

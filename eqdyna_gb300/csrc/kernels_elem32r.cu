@@ -45,8 +45,9 @@ struct RecInterior {
   static constexpr int FS = 0;                           // 24 rows of per-corner forces (overlay)
   static constexpr int NS = 24;
   static constexpr bool IDS = false;                     // node ids re-read by the gather
-  // the slot table (2 KB) overlays force rows 20-23 (written last, after a barrier that follows
-  // the reads of every slot): 10 CTAs per SM instead of 9 on C1
+  // the slot table (2 KB, copied with the tile) overlays force rows 20-23: word column e of the
+  // table holds element e's slots only (slot_index), and each thread reads its slots before it
+  // writes its own forces there; 10 CTAs per SM instead of 9 on C1
   static constexpr int SLOT = 20;
   static_assert(N <= SLOT, "slot rows clear of the copied rows");
 };
@@ -144,8 +145,9 @@ __device__ __forceinline__ void interior_rec_body(const ElemArgs32 &a, int tile)
   const int ld = g.ld;
   if (tid == 0) {
     mbar_init(&bar, 1);
-    mbar_expect_tx(&bar, (unsigned)(L::N * kTile * 4 + 8 * kTile * 2));
+    mbar_expect_tx(&bar, (unsigned)(L::N * kTile * 4 + 2 * (8 * kTile * 2)));
     bulk_g2s(sinc, g.tile_inc + (size_t)tile * kTile * 8, 8 * kTile * 2, &bar);
+    bulk_g2s(slot_of, g.tile_slot + (size_t)tile * kTile * 8, 8 * kTile * 2, &bar);
     copy_rows(tab, L::STR, g.stress, QM ? 12 : 6, ld, e0, &bar);
     if (PLASTIC) copy_rows(tab, L::POR, g.porep, 1, ld, e0, &bar);
     copy_rows(tab, L::RID, g.rec_id, 1, ld, e0, &bar);
@@ -156,13 +158,10 @@ __device__ __forceinline__ void interior_rec_body(const ElemArgs32 &a, int tile)
   const bool ok = mbar_wait_bounded(&bar, a.err);
   const unsigned short *incp = ts.sincp;
   if (__syncthreads_or(!ok)) return;  // the whole CTA skips the tile if any thread gave up
-  build_slots(incp, M, sinc, slot_of);  // reads the staged pointers of other threads
-  __syncthreads();
   const int e = e0 + tid;
   float *fs = tab + L::FS * kTile;
   int sl[8];
-  load_slots(slot_of, tid, sl);
-  __syncthreads();  // every slot read before the force rows over the slot table are written
+  load_slots(slot_of, tid, sl);  // column tid of the slot rows is this thread's own: no barrier
   if (tid < live) {
     double *ps = PLASTIC ? g.pstrain + e : nullptr;
     if (UNI) {
@@ -210,8 +209,8 @@ __device__ __forceinline__ void pml_rec_body(const ElemArgs32 &a, int tile) {
   const bool ok = mbar_wait_bounded(&bar, a.err);
   const unsigned short *incp = ts.sincp;
   if (__syncthreads_or(!ok)) return;  // the whole CTA skips the tile if any thread gave up
-  build_slots(incp, M, sinc, slot_of);  // reads the staged pointers of other threads
-  __syncthreads();
+  build_slots(incp, M, sinc, slot_of);  // reads the staged pointers of other threads (the slot table
+  __syncthreads();                      // costs the PML pass more as a copy than built here)
   const int e = e0 + tid;
   float *cfh = tab + L::FS * kTile;
   float *es = tab + L::ES * kTile;
