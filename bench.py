@@ -62,8 +62,9 @@ NODE_BYTES = {"fp64": (152, 536), "fp32": (148, 340)}
 # DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) per element of the binary32
 # kernels on a uniform grid (one record per group), from the ncu capture of C1 at dx = 200 m
 # (profiles/elem_f32_uniform_C1-dx200.md), scaled to a launch by its element count.
-NCU_TRAFFIC_PER_UNIT = {("elem_interior", "records", 1): (112.008448e6 + 11.831808e6) / 1125000,
-                        ("elem_pml", "records", 1): (283.672832e6 + 106.202880e6) / 1402000,
+# (the interior pass also reads the 2 KB slot table of each tile, about 18 B per element)
+NCU_TRAFFIC_PER_UNIT = {("elem_interior", "records", 1): (132.438272e6 + 16.760320e6) / 1125000,
+                        ("elem_pml", "records", 1): (283.675648e6 + 104.746752e6) / 1402000,
                         # per node of the C1 mesh at dx = 200 m (55 % PML nodes; C1 at 100 m: 56 %)
                         ("node_update", None, None): (299.577856e6 + 298.804992e6) / 2592757}
 JOB_STEPS = {"C0": 1000, "C1": 4000, "C2": 6000, "C3": 5000}
