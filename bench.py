@@ -470,7 +470,8 @@ def bench_ours(args, world, rank, local):
                                           for k, v in tables.items()},
                        "launch": launch or "defaults",
                        "parallelism": "replicas" if world > 1 else "single GPU",
-                       "setup_s": round(setup_s, 1), "wall_ms_per_step": wall * 1e3 / args.steps,
+                       "setup_s": round(setup_s, 1), "setup_phases_s": case.build_phases_s,
+                       "wall_ms_per_step": wall * 1e3 / args.steps,
                        "timing": "value: CUDA events around the K-step call on the library's stream (16-step "
                                  "graphs, fault phase beside the next node update); kernel shares and "
                                  "rooflines: per-launch events over up to 40 steps in the reference's order",

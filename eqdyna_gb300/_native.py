@@ -125,6 +125,8 @@ def case_lib():
         lib.eqd_case_dims.restype = C.c_int
         lib.eqd_case_lines.argtypes = [C.c_void_p] + [C.POINTER(c_double_p)] * 3
         lib.eqd_case_lines.restype = C.c_int
+        lib.eqd_case_phase_seconds.argtypes = [C.c_void_p, c_double_p]
+        lib.eqd_case_phase_seconds.restype = C.c_int
         lib.eqd_case_free.argtypes = [C.c_void_p]
         lib.eqd_case_free.restype = None
         lib.eqd_case_last_error.argtypes = []
@@ -223,7 +225,7 @@ GPU_SYMBOLS = ["eqd_gpu_init", "eqd_gpu_step", "eqd_gpu_fetch", "eqd_gpu_fetch_f
                "eqd_gpu_mlp_set", "eqd_gpu_mlp_enable", "eqd_gpu_newton_replay", "eqd_mlp_gradient",
                "eqd_gpu_fp64_fma_peak", "eqd_gpu_check_conversions"]
 CASE_SYMBOLS = ["eqd_case_build", "eqd_case_view", "eqd_case_array_len", "eqd_case_dims",
-                "eqd_case_lines", "eqd_case_free", "eqd_case_last_error"]
+                "eqd_case_lines", "eqd_case_phase_seconds", "eqd_case_free", "eqd_case_last_error"]
 
 
 class PinnedArray:

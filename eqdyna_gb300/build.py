@@ -56,7 +56,7 @@ def build_case(force=False):
     deps = [src, os.path.join(INCLUDE, "eqdyna_case.h"), os.path.join(INCLUDE, "eqdyna_gb300.h")]
     if force or _newer(CASE_LIB, deps):
         os.makedirs(LIBDIR, exist_ok=True)
-        _run(["g++", *HOST_FLAGS, "-shared", src, "-o", CASE_LIB])
+        _run(["g++", *HOST_FLAGS, "-fopenmp", "-shared", src, "-o", CASE_LIB])
     return CASE_LIB
 
 

@@ -14,6 +14,7 @@ import ctypes as C
 import json
 import os
 import tempfile
+import time
 
 import numpy as np
 
@@ -115,6 +116,25 @@ def write_case_dir(path, params, material, st_on_fault, st_off_fault, on_fault_v
     return path
 
 
+class _NativeCase:
+    """Owns a built case's native arrays; the case is freed when the last array viewing them is
+    gone, so that the arrays are handed out without a copy."""
+
+    def __init__(self, lib, handle):
+        self.lib, self.handle = lib, handle
+
+    def view(self, ptr, n, dtype):
+        ctype = C.c_int32 if dtype == np.int32 else C.c_double
+        buf = (ctype * n).from_address(C.cast(ptr, C.c_void_p).value)
+        buf._owner = self
+        return np.frombuffer(buf, dtype=dtype)
+
+    def __del__(self):
+        if self.handle:
+            self.lib.eqd_case_free(self.handle)
+            self.handle = None
+
+
 class Case:
     """Fortran-layout state of one case (the globalvar arrays after setup)."""
 
@@ -125,14 +145,17 @@ class Case:
         self.dims = dims
         self.lines = lines
         self.directory = directory
+        self.build_phases_s = None
 
     @classmethod
     def from_dir(cls, path):
         lib = N.case_lib()
         h = C.c_void_p()
+        t0 = time.perf_counter()
         rc = lib.eqd_case_build(os.fsencode(path), C.byref(h))
         if rc != 0:
             raise N.EqdError(rc, "eqd_case_build", lib.eqd_case_last_error().decode())
+        owner = _NativeCase(lib, h)
         try:
             sc = N.EqdScalars()
             ha = N.EqdHostArrays()
@@ -145,8 +168,7 @@ class Case:
                 if n == 0 or not ptr:
                     arrays[name] = None
                     continue
-                dt = np.int32 if name in N.INT_ARRAYS else np.float64
-                arrays[name] = np.ctypeslib.as_array(ptr, shape=(n,)).astype(dt, copy=True)
+                arrays[name] = owner.view(ptr, n, np.int32 if name in N.INT_ARRAYS else np.float64)
             sizes = {k: getattr(ha, k) for k in ("nnode", "nelem", "neq", "size_eqidx",
                                                   "size_stress", "ntotft", "nftmx",
                                                   "numOnFaultSt", "numOffFaultSt")}
@@ -160,9 +182,15 @@ class Case:
             lines = (np.ctypeslib.as_array(xs, shape=(nx.value,)).copy(),
                      np.ctypeslib.as_array(ys, shape=(ny.value,)).copy(),
                      np.ctypeslib.as_array(zs, shape=(nz.value,)).copy())
+            ph = (C.c_double * 5)()
+            lib.eqd_case_phase_seconds(h, ph)
         finally:
-            lib.eqd_case_free(h)
-        return cls(sc, arrays, sizes, dims, lines, directory=path)
+            del owner  # the builder's memory lives on in the arrays viewing it
+        case = cls(sc, arrays, sizes, dims, lines, directory=path)
+        case.build_phases_s = dict(zip(("inputs", "mesh", "fault", "element_tables", "finish"),
+                                       (round(v, 3) for v in ph)))
+        case.build_phases_s["views"] = round(time.perf_counter() - t0 - sum(ph), 3)
+        return case
 
     @classmethod
     def from_fixture(cls, npz_path, workdir=None, overrides=None, gpu_switches=None):

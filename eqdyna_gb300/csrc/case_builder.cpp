@@ -17,6 +17,8 @@
 //   initial split-node vel .... src/eqdyna3d.f90:191-212 (init_vel)
 #include "eqdyna_case.h"
 
+#include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -314,6 +316,36 @@ void read_inputs(const std::string &dir, Inputs &in) {
 }
 
 // ---------------------------------------------------------------------------------------------
+// Allocator that leaves new elements uninitialised: the large tables are written in parallel
+// loops, so that their pages are first touched by the threads that fill them.
+template <class T>
+struct DefaultInit : std::allocator<T> {
+  template <class U>
+  struct rebind {
+    using other = DefaultInit<U>;
+  };
+  DefaultInit() = default;
+  template <class U>
+  DefaultInit(const DefaultInit<U> &) noexcept {}
+  template <class U>
+  void construct(U *) noexcept {}
+  template <class U, class... Args>
+  void construct(U *p, Args &&...args) {
+    ::new ((void *)p) U(std::forward<Args>(args)...);
+  }
+};
+template <class T>
+using Table = std::vector<T, DefaultInit<T>>;
+
+// parallel zero fill (first touch by many threads)
+template <class V>
+void zero_fill(V &v, size_t n) {
+  v.resize(n);
+  double *p = v.data();
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < static_cast<int64_t>(n); ++i) p[i] = 0.0;
+}
+
 struct Case {
   Inputs in;
   eqd_scalars sc{};
@@ -332,11 +364,11 @@ struct Case {
   std::vector<int32_t> nodeElemIdRelation;  // (8, nelem)
   std::vector<int32_t> elemTypeArr, stressCompIndexArr;
   std::vector<double> matRows;               // [e*5 + k]
-  std::vector<double> mat;                   // (nelem, 5)
+  Table<double> mat;                         // (nelem, 5)
   std::vector<double> stressArr;
   int64_t stressDofCount = 0;
-  std::vector<double> eleporep, pstrain, eledet, elemass, eleshp, ss, phi;
-  std::vector<double> nodalMassArr, fnms, v1, velArr, dispArr, nodalForceArr;
+  std::vector<double> eleporep, pstrain, nodalMassArr, fnms;
+  Table<double> eledet, elemass, eleshp, ss, phi, v1, velArr, dispArr, nodalForceArr;
   // fault
   int32_t nftnd = 0;
   std::vector<int32_t> nsmp;                 // (2, nftnd)
@@ -347,6 +379,8 @@ struct Case {
   std::vector<int32_t> fltrc;                // (2, nxuni, nzuni)
   int ixfi = 0, izfi = 0, ifs = 0, ifd = 0;
   std::unordered_map<int32_t, int32_t> slave_to_master;
+  std::vector<char> station_level;           // (nz): an off-fault station lies at this depth
+  std::vector<int32_t> cell_plane_start;     // (nx + 2): first element of each x-layer of cells
   // stations
   std::vector<int32_t> anonfs;               // (3, nOnFound)
   std::vector<int32_t> offStIndex;           // (2, nOffFound): station i, node id
@@ -484,10 +518,11 @@ bool near_line(double s, double node, double lo_line, double hi_line, bool use_l
   return false;
 }
 
-void surface_station(Case &c, int ix, int iy, const double p[3], int nodeId) {
+void surface_station(Case &c, int ix, int iy, int iz, const double p[3], int nodeId) {
   const Inputs &in = c.in;
   const int nx = c.nx, ny = c.ny;
   if (!(iy > 1 && iy < ny)) return;
+  if (!c.station_level[iz - 1]) return;  // no station within kTol of this grid level's depth
   int part;
   if (ix > 1 && ix < nx) part = 1;
   else if (ix == 1) part = 2;
@@ -681,18 +716,43 @@ void mesh(Case &c) {
   c.ny = static_cast<int>(c.yline.size());
   c.nz = static_cast<int>(c.zline.size());
   const int nxyz = c.nx * c.ny * c.nz;
+  {
+    // split nodes are numbered after the grid's nodes: room for one per uniform fault cell
+    const size_t nodes = static_cast<size_t>(nxyz) + static_cast<size_t>(c.nxuni) * c.nzuni + 16;
+    c.eqNumStartIndexLoc.reserve(nodes);
+    c.numOfDofPerNodeArr.reserve(nodes);
+    c.meshCoor.reserve(3 * nodes);
+  }
   c.eqNumStartIndexLoc.assign(nxyz, 0);
   c.numOfDofPerNodeArr.assign(nxyz, 0);
   c.meshCoor.assign(static_cast<size_t>(3) * nxyz, 0.0);
   c.fltrc.assign(static_cast<size_t>(2) * c.nxuni * c.nzuni, 0);
   c.n4yn.assign(in.nOffSt, 0);
+  c.station_level.assign(c.nz, 0);
+  for (int iz = 1; iz <= c.nz; ++iz)
+    for (int i = 0; i < in.nOffSt; ++i)
+      if (std::fabs(c.zline[iz - 1] - in.x4nds[3 * i + 2]) < kTol) c.station_level[iz - 1] = 1;
+  {
+    // capacity for one hexahedron per grid cell (wedges and split nodes may still grow these);
+    // reserved pages are not touched until they are filled
+    const size_t cells = static_cast<size_t>(c.nx - 1) * (c.ny - 1) * (c.nz - 1);
+    c.eqNumIndexArr.reserve(static_cast<size_t>(12) * nxyz);
+    c.nodeElemIdRelation.reserve(8 * cells);
+    c.elemTypeArr.reserve(cells);
+    c.stressCompIndexArr.reserve(cells);
+    c.matRows.reserve(5 * cells);
+    c.eleporep.reserve(cells);
+    c.stressArr.reserve(21 * cells);
+  }
   // plane1/plane2: node ids of the previous / current x-plane, indexed (iy, iz), 1-based
   std::vector<int32_t> plane1(static_cast<size_t>(c.ny + 1) * (c.nz + 1), 0), plane2 = plane1;
   auto P = [&](std::vector<int32_t> &pl, int iy, int iz) -> int32_t & {
     return pl[static_cast<size_t>(iy) + static_cast<size_t>(c.ny + 1) * iz];
   };
   int nodeCount = 0, elemCount = 0;
+  c.cell_plane_start.assign(c.nx + 2, 1);
   for (int ix = 1; ix <= c.nx; ++ix) {
+    c.cell_plane_start[ix] = elemCount + 1;  // first element of the cells between planes ix-1, ix
     for (int iz = 1; iz <= c.nz; ++iz) {
       for (int iy = 1; iy <= c.ny; ++iy) {
         const double p[3] = {c.xline[ix - 1], c.yline[iy - 1], c.zline[iz - 1]};
@@ -712,7 +772,7 @@ void mesh(Case &c) {
         c.eqNumStartIndexLoc[nodeCount - 1] = static_cast<int32_t>(c.eqNumIndexArr.size());
         c.numOfDofPerNodeArr[nodeCount - 1] = ndofNode;
         set_equation_numbers(c, p, ndofNode);
-        surface_station(c, ix, iy, p, nodeCount);
+        surface_station(c, ix, iy, iz, p, nodeCount);
         create_master_node(c, ix, iy, iz, p, nodeCount);
         if (ix >= 2 && iy >= 2 && iz >= 2) {
           // createElement, src/meshgen.f90:702-741
@@ -800,6 +860,7 @@ void mesh(Case &c) {
     const double *m = &c.matRows[5 * static_cast<size_t>(e)];
     if (m[0] == 0.0 || m[1] == 0.0 || m[2] == 0.0) fail("element without material property");
   }
+  c.cell_plane_start[c.nx + 1] = nelem + 1;
   c.pstrain.assign(nelem, 0.0);
   c.eleporep.resize(nelem, 0.0);
   c.stressArr.resize(std::max<int64_t>(c.stressDofCount, 1), 0.0);
@@ -872,11 +933,12 @@ void element_tables(Case &c) {
   const Inputs &in = c.in;
   const int nelem = static_cast<int>(c.elemTypeArr.size());
   const int nnode = static_cast<int>(c.eqNumStartIndexLoc.size());
-  c.eledet.assign(nelem, 0.0);
-  c.elemass.assign(static_cast<size_t>(24) * nelem, 0.0);
-  c.eleshp.assign(static_cast<size_t>(24) * nelem, 0.0);
-  c.ss.assign(static_cast<size_t>(6) * nelem, 0.0);
-  c.phi.assign(static_cast<size_t>(32) * nelem, 0.0);
+  // every entry is written by the element loop below
+  c.eledet.resize(nelem);
+  c.elemass.resize(static_cast<size_t>(24) * nelem);
+  c.eleshp.resize(static_cast<size_t>(24) * nelem);
+  c.ss.resize(static_cast<size_t>(6) * nelem);
+  c.phi.resize(static_cast<size_t>(32) * nelem);
   c.nodalMassArr.assign(std::max(c.equationNumCount, 1), 0.0);
   c.fnms.assign(nnode, 0.0);
   // one-point local derivatives (src/calcLocalShapeFunc.f90): corner signs
@@ -885,6 +947,10 @@ void element_tables(Case &c) {
   static const int ha[4][8] = {{1, 1, -1, -1, -1, -1, 1, 1}, {1, -1, -1, 1, -1, 1, 1, -1},
                                {1, -1, 1, -1, 1, -1, 1, -1}, {-1, 1, -1, 1, 1, -1, 1, -1}};
   const double w = 8.0;
+  // Per-element tables are independent: computed in parallel.  The first element with a
+  // non-positive determinant is reported after the loop (an exception cannot leave it).
+  int bad = nelem + 1;
+#pragma omp parallel for schedule(static) reduction(min : bad)
   for (int e = 1; e <= nelem; ++e) {
     double xl[3][8];
     for (int k = 0; k < 8; ++k)
@@ -920,7 +986,10 @@ void element_tables(Case &c) {
     const double c32 = xs[0][2] * xs[1][0] - xs[0][0] * xs[1][2];
     const double c33 = xs[0][0] * xs[1][1] - xs[0][1] * xs[1][0];
     const double det = xs[0][0] * c11 + xs[0][1] * c12 + xs[0][2] * c13;
-    if (det <= 0.0) fail("non-positive determinant at element " + std::to_string(e));
+    if (!(det > 0.0)) {
+      bad = std::min(bad, e);
+      continue;
+    }
     double gs[4][8];
     for (int k = 0; k < 8; ++k) {
       gs[0][k] = (g[0][k] * c11 + g[1][k] * c12 + g[2][k] * c13) / det;
@@ -942,32 +1011,9 @@ void element_tables(Case &c) {
       work[k] = t2;
     }
     const double t1 = totmas / dsum;
-    double em[24];
+    double *em = &c.elemass[24 * static_cast<size_t>(e - 1)];
     for (int k = 0; k < 8; ++k)
       for (int q = 0; q < 3; ++q) em[3 * k + q] = t1 * work[k];
-    // nodal mass, src/assembleGlobalMass.f90:283-326
-    for (int k = 0; k < 8; ++k) {
-      const int nid = conn(c, e, k + 1);
-      const int loc = c.eqNumStartIndexLoc[nid - 1];
-      if (c.numOfDofPerNodeArr[nid - 1] == 12) {
-        for (int q = 0; q < 3; ++q) {
-          for (int d = 3 * q; d < 3 * q + 3; ++d) {
-            const int eq = c.eqNumIndexArr[loc + d];
-            if (eq > 0) c.nodalMassArr[eq - 1] += em[3 * k + q];
-          }
-          const int eq = c.eqNumIndexArr[loc + q + 9];
-          if (eq > 0) c.nodalMassArr[eq - 1] += em[3 * k + q];
-        }
-      } else {
-        for (int q = 0; q < 3; ++q) {
-          const int eq = c.eqNumIndexArr[loc + q];
-          if (eq > 0) c.nodalMassArr[eq - 1] += em[3 * k + q];
-          else fail("3-DOF node with a fixed DOF is not supported");
-        }
-      }
-      c.fnms[nid - 1] += em[3 * k];
-    }
-    for (int q = 0; q < 24; ++q) c.elemass[24 * static_cast<size_t>(e - 1) + q] = em[q];
     c.eledet[e - 1] = det;
     for (int k = 0; k < 8; ++k)
       for (int q = 0; q < 3; ++q) c.eleshp[24 * static_cast<size_t>(e - 1) + 3 * k + q] = gs[q][k];
@@ -998,6 +1044,49 @@ void element_tables(Case &c) {
       for (int j = 0; j < 8; ++j) ph[8 * mode + j] = pm[j] / nrm;
     }
   }
+  if (bad <= nelem) fail("non-positive determinant at element " + std::to_string(bad));
+  // nodal mass, src/assembleGlobalMass.f90:283-326.  The reference adds the element masses
+  // element by element; every sum here is taken in that order.  Nodes are numbered x-plane by
+  // x-plane (a split node lies in the plane of its grid node) and the elements of a layer of cells
+  // touch only its two bounding planes, so the nodes of plane j receive contributions only from
+  // layers j and j + 1: each plane is assembled on its own, in element order.
+  const int plane_nodes = c.ny * c.nz, nxyz = c.nx * c.ny * c.nz;
+  std::vector<int32_t> split_plane(c.nftnd);
+  for (int k = 0; k < c.nftnd; ++k) split_plane[k] = (c.nsmp[2 * k] - 1) / plane_nodes + 1;
+  auto plane_of = [&](int nid) {
+    return nid <= nxyz ? (nid - 1) / plane_nodes + 1 : split_plane[nid - nxyz - 1];
+  };
+  int fixed_dof = 0;
+#pragma omp parallel for schedule(dynamic, 1) reduction(max : fixed_dof)
+  for (int j = 1; j <= c.nx; ++j) {
+    const int e_end = c.cell_plane_start[std::min(j + 1, c.nx) + 1];
+    for (int e = c.cell_plane_start[j]; e < e_end; ++e) {
+      const double *em = &c.elemass[24 * static_cast<size_t>(e - 1)];
+      for (int k = 0; k < 8; ++k) {
+        const int nid = conn(c, e, k + 1);
+        if (plane_of(nid) != j) continue;
+        const int loc = c.eqNumStartIndexLoc[nid - 1];
+        if (c.numOfDofPerNodeArr[nid - 1] == 12) {
+          for (int q = 0; q < 3; ++q) {
+            for (int d = 3 * q; d < 3 * q + 3; ++d) {
+              const int eq = c.eqNumIndexArr[loc + d];
+              if (eq > 0) c.nodalMassArr[eq - 1] += em[3 * k + q];
+            }
+            const int eq = c.eqNumIndexArr[loc + q + 9];
+            if (eq > 0) c.nodalMassArr[eq - 1] += em[3 * k + q];
+          }
+        } else {
+          for (int q = 0; q < 3; ++q) {
+            const int eq = c.eqNumIndexArr[loc + q];
+            if (eq > 0) c.nodalMassArr[eq - 1] += em[3 * k + q];
+            else fixed_dof = 1;
+          }
+        }
+        c.fnms[nid - 1] += em[3 * k];
+      }
+    }
+  }
+  if (fixed_dof) fail("3-DOF node with a fixed DOF is not supported");
   // wedge sanity check, src/assembleGlobalMass.f90:43-55
   for (int e = 1; e <= nelem; ++e) {
     const int et = c.elemTypeArr[e - 1];
@@ -1011,15 +1100,17 @@ void finish(Case &c) {
   const int nelem = static_cast<int>(c.elemTypeArr.size());
   const int neq = std::max(c.equationNumCount, 1);
   // mat (nelem, 5), column-major
-  c.mat.assign(static_cast<size_t>(5) * nelem, 0.0);
+  c.mat.resize(static_cast<size_t>(5) * nelem);
+#pragma omp parallel for schedule(static)
   for (int e = 0; e < nelem; ++e)
     for (int k = 0; k < 5; ++k) c.mat[static_cast<size_t>(k) * nelem + e] = c.matRows[5 * static_cast<size_t>(e) + k];
+  std::vector<double>().swap(c.matRows);  // the case lives as long as its arrays: drop the copy
   c.n_phys_elem = 0;
   for (int e = 0; e < nelem; ++e) c.n_phys_elem += (c.elemTypeArr[e] != 2);
-  c.v1.assign(neq, 0.0);
-  c.nodalForceArr.assign(neq, 0.0);
-  c.velArr.assign(static_cast<size_t>(3) * nnode, 0.0);
-  c.dispArr.assign(static_cast<size_t>(3) * nnode, 0.0);
+  zero_fill(c.v1, neq);
+  zero_fill(c.nodalForceArr, neq);
+  zero_fill(c.velArr, static_cast<size_t>(3) * nnode);
+  zero_fill(c.dispArr, static_cast<size_t>(3) * nnode);
   // init_vel, src/eqdyna3d.f90:191-212
   for (int i = 1; i <= c.nftnd; ++i) {
     const double *f = &c.fric[100 * static_cast<size_t>(i - 1) - 1];
@@ -1093,6 +1184,7 @@ void finish(Case &c) {
 
 struct eqd_case {
   Case c;
+  double phase_s[5] = {0, 0, 0, 0, 0};  // inputs, mesh, on-fault fields, element tables, finish
 };
 
 extern "C" {
@@ -1104,11 +1196,22 @@ int eqd_case_build(const char *dir, eqd_case **out) {
   *out = nullptr;
   auto *h = new eqd_case();
   try {
+    auto t = std::chrono::steady_clock::now();
+    auto lap = [&](int k) {
+      const auto now = std::chrono::steady_clock::now();
+      h->phase_s[k] = std::chrono::duration<double>(now - t).count();
+      t = now;
+    };
     read_inputs(dir, h->c.in);
+    lap(0);
     mesh(h->c);
+    lap(1);
     on_fault_fields(h->c);
+    lap(2);
     element_tables(h->c);
+    lap(3);
     finish(h->c);
+    lap(4);
   } catch (const CaseError &e) {
     g_case_error = e.what();
     delete h;
@@ -1246,6 +1349,12 @@ int eqd_case_lines(eqd_case *h, const double **x, const double **y, const double
   if (x) *x = h->c.xline.data();
   if (y) *y = h->c.yline.data();
   if (z) *z = h->c.zline.data();
+  return EQD_OK;
+}
+
+int eqd_case_phase_seconds(eqd_case *h, double out[5]) {
+  if (!h || !out) return EQD_ERR_INPUT;
+  for (int k = 0; k < 5; ++k) out[k] = h->phase_s[k];
   return EQD_OK;
 }
 

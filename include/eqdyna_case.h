@@ -45,6 +45,10 @@ int eqd_case_dims(eqd_case *c, int32_t *nx, int32_t *ny, int32_t *nz, int64_t *n
 /* Grid-line coordinates (x, y, z node lines) of the structured grid. */
 int eqd_case_lines(eqd_case *c, const double **x, const double **y, const double **z);
 
+/* Wall seconds of the build's phases: input files, mesh generation, on-fault fields, element
+ * tables, mass assembly and finishing. */
+int eqd_case_phase_seconds(eqd_case *c, double out[5]);
+
 void eqd_case_free(eqd_case *c);
 const char *eqd_case_last_error(void);
 

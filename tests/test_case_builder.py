@@ -86,3 +86,33 @@ def test_split_nodes(tpv8):
     assert np.array_equal(uses_slave, on_fault.any(axis=1) & ~reachable)
     # fault areas sum to the fault area
     assert c.arrays["arn"].sum() == pytest.approx(30e3 * 15e3, rel=1e-12)
+
+
+_HASH_SCRIPT = """
+import hashlib, sys, tempfile
+from eqdyna_gb300 import configs
+from eqdyna_gb300.case import Case
+d = tempfile.mkdtemp(prefix="eqd_thr_")
+configs.CONFIGS[sys.argv[1]](d, scale=float(sys.argv[2]), nsteps=20)
+c = Case.from_dir(d)
+for k, v in sorted(c.arrays.items()):
+    print(k, None if v is None else hashlib.sha1(v.tobytes()).hexdigest())
+"""
+
+
+@pytest.mark.parametrize("config,scale", [("C0", 4.0), ("C3", 8.0)])
+def test_tables_independent_of_thread_count(config, scale):
+    """The parallel setup (per-element tables, nodal masses assembled plane by plane in element
+    order, parallel first touch) gives the same bytes with one host thread as with all of them."""
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    out = []
+    for threads in ("1", str(max(os.cpu_count() or 2, 2))):
+        env = dict(os.environ, OMP_NUM_THREADS=threads, PYTHONPATH=root)
+        r = subprocess.run([sys.executable, "-c", _HASH_SCRIPT, config, str(scale)], env=env,
+                           capture_output=True, text=True, timeout=600, cwd=root)
+        assert r.returncode == 0, r.stderr
+        out.append(r.stdout)
+    assert out[0] == out[1] and "nodalMassArr" in out[0]
