@@ -293,7 +293,12 @@ def bench_ours(args, world, rank, local):
     from eqdyna_gb300.autotune import tuned_options
     launch = tuned_options(args.config, local) if (args.tuned and args.precision == "fp32") else {}
     args.learned = int(bool(args.learned) and case.scalars.friclaw in (3, 4))  # rate-and-state only
-    nlog = min(args.log_steps * args.log_stride, job) if args.learned else 0
+    log_stride, log_steps = args.log_stride, args.log_steps
+    if args.learned and log_steps * log_stride > job // 2:
+        # a short job: the logged warm-up takes about half of it (one step in log_stride)
+        log_stride = max(1, min(log_stride, job // 4))
+        log_steps = max(1, (job // 2) // log_stride)
+    nlog = log_steps * log_stride if args.learned else 0
 
     # ---- end to end: the whole job through the C ABI with host buffers ----
     e2e_case = case.clone()
@@ -322,7 +327,7 @@ def bench_ours(args, world, rank, local):
     done, train_s, hist, warm_s = 0, 0.0, None, 0.0
     if args.learned:  # plain warm-up whose Newton solves are the training data, then training
         t1 = time.perf_counter()
-        s.newton_log(nlog // args.log_stride, args.log_stride)
+        s.newton_log(nlog // log_stride, log_stride)
         run_steps(nlog)
         done = nlog
         warm_s = time.perf_counter() - t1
@@ -344,8 +349,8 @@ def bench_ours(args, world, rank, local):
         plain = s.replay(learned=False)
         guess = s.replay(learned=True)
         params, norm = s.mlp_state()
-        learned = {"records": plain["records"], "logged_steps": nlog // args.log_stride,
-                   "log_stride": args.log_stride, "train_s": round(train_s, 2), "epochs": args.epochs,
+        learned = {"records": plain["records"], "logged_steps": nlog // log_stride,
+                   "log_stride": log_stride, "train_s": round(train_s, 2), "epochs": args.epochs,
                    "epoch_loss": [round(x, 5) for x in hist["epoch_loss"]],
                    "holdout_loss": round(hist["holdout_loss"], 5),
                    "replay_plain_guess": plain, "replay_learned_guess": guess, "job_newton": job_newton}

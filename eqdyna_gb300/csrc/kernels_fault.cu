@@ -916,7 +916,10 @@ int launch_fault(Context &c, cudaStream_t s, bool overlapped) {
   const int grid = (nthreads + bf - 1) / bf;
   if (overlapped) {
     // beside the PML pass: the launch carries the highest priority itself, so that a captured
-    // graph node keeps it (a graph does not take the priority of the capturing stream)
+    // graph node keeps it (a graph does not take the priority of the capturing stream).  (One
+    // single-warp CTA per SM, which fits beside a full complement of PML CTAs, was slower: each
+    // warp's 20-iteration binary64 solves are latency-bound, and six rounds of them outlast the
+    // PML pass, 2.61 -> 3.05 ms per C1 step.)
     int lo = 0, hi = 0;
     cudaDeviceGetStreamPriorityRange(&lo, &hi);
     cudaLaunchAttribute attr[1];

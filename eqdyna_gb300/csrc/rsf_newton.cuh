@@ -84,7 +84,7 @@ __device__ __forceinline__ NewtonOut rsf_newton(int friclaw, double dt, const Ne
                                   : 1.0 / (2.0 * p.V0) * exp(s.state0 / p.A);
   double v_eval = v0;                        // FAST: where the law was last evaluated
   double vA = 0.0, thA = 0.0, tcA = 0.0;     // FAST: v_(k-2) and the law evaluated at it
-  double step = 0.0;
+  double dv_last = 0.0, vt_last = 1.0;       // Newton step and iterate of the last evaluation
   int iv, executed = 0;
   for (iv = 1; iv <= 20; ++iv) {
     ++executed;
@@ -111,9 +111,11 @@ __device__ __forceinline__ NewtonOut rsf_newton(int friclaw, double dt, const Ne
       rsfeq = vt + s.Tc * (taoc_new * 0.5 - s.trial);
       dr = 1.0 + s.Tc * (-dxmudv * fmin(s.tn, 0.0)) * 0.5;
     }
-    step = fabs(rsfeq / dr) / fabs(vt);
-    if (fabs(rsfeq / dr) < 1.e-14 * fabs(vt) && fabs(rsfeq) < 1.e-6 * fabs(vt)) break;
-    const double vn = vt - rsfeq / dr;
+    const double dv = rsfeq / dr;
+    dv_last = dv;
+    vt_last = vt;
+    if (fabs(dv) < 1.e-14 * fabs(vt) && fabs(rsfeq) < 1.e-6 * fabs(vt)) break;
+    const double vn = vt - dv;
     const double vnew = (vn <= 0.0) ? vt / 2.0 : vn;
     if (FAST && iv < 20) {
       if (vnew == vt) {  // fixed point: v_20 = v_19 = vt
@@ -140,6 +142,8 @@ __device__ __forceinline__ NewtonOut rsf_newton(int friclaw, double dt, const Ne
     vt = vnew;
   }
   if (FAST) stateTmp = rsf_state(friclaw, v_eval, s.state0, p, dt);
+  // the step ratio of the last evaluation, formed once here rather than in every iteration
+  const double step = fabs(dv_last) / fabs(vt_last);
   NewtonOut o;
   o.v = vt;
   o.state = stateTmp;
