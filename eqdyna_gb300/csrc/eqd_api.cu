@@ -348,9 +348,11 @@ class RecordDict {
   std::vector<float> rows_;
 };
 
-// Auto layout: record-indexed when a group has at most this many distinct records (the table then
-// stays L2-resident) and at most half as many records as elements.
-constexpr long kAutoMaxRecords = 65536;
+// Auto layout: record-indexed when a group's distinct records fit in a third of the 129 MB L2
+// (48 MB: C3's sheared and stretched cells have ~100k records of ~280 bytes per element group at
+// dx = 100 m) and there are at most half as many records as elements.
+constexpr long kAutoRecordBytes = 48l << 20;
+inline long auto_max_records(int record_floats) { return kAutoRecordBytes / (4l * record_floats); }
 
 // binary32 copy of a component-major table [ncomp][m] with its rows padded with zeros to stride ld
 template <class V>
@@ -666,7 +668,7 @@ int build_device_state(eqd_context &X, const eqd_scalars &s, const eqd_host_arra
       std::vector<float> abt;
       if (use_rec) {
         // per-thread dictionaries over contiguous chunks, merged in chunk order
-        const long cap = (layout == EQD_TABLES_RECORDS || qm) ? (long)m : std::min<long>(kAutoMaxRecords, m / 2 + 1);
+        const long cap = (layout == EQD_TABLES_RECORDS || qm) ? (long)m : std::min<long>(auto_max_records(dict.len()), m / 2 + 1);
         rid.assign(ld, 0u);
         const int T = std::max(1, omp_get_max_threads());
         std::vector<RecordDict> local(T, RecordDict(dict.len()));

@@ -63,9 +63,16 @@ def test_logged_solves_replay_bit_for_bit(c1_logged):
     assert fast["executed"] <= ref["executed"]
 
 
-def test_learned_guess_trains_and_converges_to_the_same_solutions(c1_logged):
-    s, _ = c1_logged
+@pytest.fixture(scope="module")
+def c1_trained(c1_logged):
+    """The model trained on the logged plain solves (once per module, whichever test asks first)."""
+    s, case = c1_logged
     hist = s.train_mlp(epochs=20, batch=1024, lr=2e-3, holdout=0.1, seed=5)
+    return s, case, hist
+
+
+def test_learned_guess_trains_and_converges_to_the_same_solutions(c1_trained):
+    s, _, hist = c1_trained
     print("loss", hist)
     assert hist["epoch_loss"][-1] < 0.5 * hist["epoch_loss"][0]
     assert hist["holdout_loss"] < 2.0 * hist["epoch_loss"][-1]
@@ -78,13 +85,13 @@ def test_learned_guess_trains_and_converges_to_the_same_solutions(c1_logged):
     s.enable_mlp(False)
 
 
-def test_fp32_learned_form_within_budget(c1_logged):
+def test_fp32_learned_form_within_budget(c1_trained):
     """The model trained on the plain solves drives the binary32 form over C1 (dx = 400 m, 300
     steps) within the slip-rate budget of the binary64 oracle."""
     from eqdyna_gb300.solver import GpuSolver
     from oracle import Oracle
     from test_gpu_fp32 import _check, _errors
-    s, case = c1_logged
+    s, case, _ = c1_trained
     params, norm = s.mlp_state()
     cpu = case.clone()
     Oracle(cpu, nthreads()).step(300)
