@@ -5,8 +5,8 @@
 // Inputs (raw features of one solve): ln V_trial (the slip rate the plain method starts from),
 // ln |state|, effective normal traction, trial shear traction, a, b.  Output: ln(V / V_trial) of the
 // converged slip rate V, so the guess is V_trial * exp(output).  The guess only replaces the
-// starting point; Newton then runs to the reference's own exit test, so the plain solve stays both
-// the fallback and the judge.
+// starting point; Newton then runs to the reference's own exit test, which still decides
+// convergence, and the plain starting point stays the fallback.
 #pragma once
 #include <cuda_runtime.h>
 #include <cuda_bf16.h>

@@ -1,6 +1,6 @@
 """GPU binary64 form vs the oracle (and vs the reference golden), through the C ABI.
 
-Bar (the benchmark spec): relative L2 <= 1e-9 on slip, slip rate and station velocities, rupture time
+Bar: relative L2 <= 1e-9 on slip, slip rate and station velocities, rupture time
 within one time step.  Element forces are summed into nodes in a different order than the
 reference (and atomically), so agreement is to round-off, not bitwise.
 """
