@@ -380,6 +380,7 @@ struct Case {
   int ixfi = 0, izfi = 0, ifs = 0, ifd = 0;
   std::unordered_map<int32_t, int32_t> slave_to_master;
   std::vector<char> station_level;           // (nz): an off-fault station lies at this depth
+  double dip_tan = 0.0, dip_norm = 1.0;      // tan(C_degen), (1 + tan^2)^(1/2): the dipping plane
   std::vector<int32_t> cell_plane_start;     // (nx + 2): first element of each x-layer of cells
   // stations
   std::vector<int32_t> anonfs;               // (3, nOnFound)
@@ -466,9 +467,9 @@ bool on_fault(const Case &c, const double p[3]) {
     return false;
   if (in.C_degen == 0.0 && p[1] == 0.0) return true;
   if (in.C_degen > 3.0) {
-    const double t = std::tan(in.C_degen / 180.0 * kPi);
+    const double t = c.dip_tan;
     double d = std::fabs(p[2] + p[1] * t);
-    d = d / std::pow(1.0 + t * t, 0.5);
+    d = d / c.dip_norm;
     if (d < in.dx / 100.0) return true;
   }
   return false;
@@ -670,8 +671,8 @@ void grow_stress(Case &c) {
 // src/library_degeneration.f90:3-55
 void wedge(Case &c, const double ctr[3], int &elemCount, int plane_ids[8]) {
   const Inputs &in = c.in;
-  const double t = std::tan(in.C_degen / 180.0 * kPi);
-  const double dist = std::fabs(ctr[1] * t + ctr[2]) / std::pow(1.0 + t * t, 0.5);
+  const double t = c.dip_tan;
+  const double dist = std::fabs(ctr[1] * t + ctr[2]) / c.dip_norm;
   if (!(ctr[0] > in.fxmin && ctr[0] < in.fxmax && ctr[1] > in.fymin && ctr[1] < in.fymax &&
         ctr[2] > in.fzmin && dist < kTol))
     return;
@@ -728,6 +729,8 @@ void mesh(Case &c) {
   c.meshCoor.assign(static_cast<size_t>(3) * nxyz, 0.0);
   c.fltrc.assign(static_cast<size_t>(2) * c.nxuni * c.nzuni, 0);
   c.n4yn.assign(in.nOffSt, 0);
+  c.dip_tan = std::tan(in.C_degen / 180.0 * kPi);
+  c.dip_norm = std::pow(1.0 + c.dip_tan * c.dip_tan, 0.5);
   c.station_level.assign(c.nz, 0);
   for (int iz = 1; iz <= c.nz; ++iz)
     for (int i = 0; i < in.nOffSt; ++i)

@@ -145,3 +145,22 @@ def test_c3_fp32_learned(c3):
         assert err_plain[k] <= 5e-2, (k, err_plain[k])
         assert err[k] <= max(1e-2, 3.0 * err_plain[k]), (k, err[k], err_plain[k])
     assert err["rupture_flips"] <= max(10, 2 * err_plain["rupture_flips"])
+
+
+def test_c3_sparse_pml_tiles_are_repacked():
+    """C3's PML shell has stretched cells: bins of the median element width merge some and skip
+    others, and with the default 4 x 8 x 4 brick about half of the PML slots would stay empty
+    (51 %).  The brick order then bins by rank (one bin per cell of a structured layer) and keeps
+    the densest candidate order."""
+    from eqdyna_gb300.case import Case
+    from eqdyna_gb300.configs import config_c3
+    from eqdyna_gb300.solver import GpuSolver
+    case = Case.from_dir(config_c3(tempfile.mkdtemp(prefix="eqd_c3t_"), scale=4.0, nsteps=10))
+    with GpuSolver(case, precision="fp32") as s:
+        info = s.table_info()
+    for name, grp in info.items():
+        live = grp["elements"] / grp["slots"]
+        print(name, grp["tiles"], "tiles", round(live, 3), "live")
+        assert grp["slots"] == 128 * grp["tiles"]
+    assert info["pml"]["elements"] / info["pml"]["slots"] >= 0.65
+    assert info["interior"]["elements"] / info["interior"]["slots"] >= 0.7
