@@ -2038,4 +2038,25 @@ int eqd_gpu_fp64_fma_peak(int32_t device, double *tflops) {
   return EQD_OK;
 }
 
+int eqd_host_element_order(const eqd_host_arrays *a, int32_t group, int32_t tile_shape, int32_t *out,
+                           int64_t cap, int64_t *n_out, double *live) {
+  if (!a || !n_out || (group != 0 && group != 1) || a->nelem < 0 || !a->elemTypeArr ||
+      !a->nodeElemIdRelation || !a->meshCoor)
+    return EQD_ERR_INPUT;
+  std::vector<int> ids;
+  for (int e = 0; e < a->nelem; ++e) {
+    const int t = a->elemTypeArr[e];
+    if (group == 0 ? (t == 1 || t > 10) : (t == 2)) ids.push_back(e);
+  }
+  const int ts = tile_shape > 0 ? tile_shape : (4 | 8 << 8 | 4 << 16);
+  const int bx = ts & 255, by = (ts >> 8) & 255, bz = (ts >> 16) & 255;
+  if (bx < 1 || by < 1 || bz < 1) return EQD_ERR_INPUT;
+  const double f = brick_order(*a, ids, bx, bz, by, eqd::tile_size_interior());
+  if (live) *live = f;
+  *n_out = (int64_t)ids.size();
+  if (!out || cap < (int64_t)ids.size()) return out ? EQD_ERR_INPUT : EQD_OK;
+  std::copy(ids.begin(), ids.end(), out);
+  return EQD_OK;
+}
+
 }  // extern "C"

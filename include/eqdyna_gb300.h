@@ -317,6 +317,14 @@ int eqd_gpu_init_times(eqd_context *ctx, double ms[8]);
  * tile; info[7] = distinct nodes summed over the tiles (the node gathers of one pass). */
 int eqd_gpu_table_info(eqd_context *ctx, int32_t group, int64_t info[8]);
 
+/* Host only (no GPU needed): the element order the binary32 form's tiles are cut from, for group
+ * 0 (interior: elemTypeArr 1 and 11-13) or 1 (PML: 2) with the given tile shape (0: default).
+ * out[0 .. *n_out) = 0-based element numbers, -1 for the empty slots that pad a brick to a tile
+ * boundary; *live = elements / slots (0 when the input order is kept).  With out == NULL only
+ * *n_out and *live are set; a cap below *n_out returns EQD_ERR_INPUT. */
+int eqd_host_element_order(const eqd_host_arrays *a, int32_t group, int32_t tile_shape, int32_t *out,
+                           int64_t cap, int64_t *n_out, double *live);
+
 /* Measured binary64 fused-multiply-add throughput of a device (TFLOP/s, 2 flops per FMA),
  * from a register-resident FMA chain kernel; used as the compute roofline of the FP64 form. */
 int eqd_gpu_fp64_fma_peak(int32_t device, double *tflops);
