@@ -116,3 +116,24 @@ def test_tables_independent_of_thread_count(config, scale):
         assert r.returncode == 0, r.stderr
         out.append(r.stdout)
     assert out[0] == out[1] and "nodalMassArr" in out[0]
+
+
+def test_arrays_outlive_the_case_and_clones_are_private():
+    """Case.from_dir hands out views of the builder's arrays without copying: an array kept after
+    its case is gone stays valid (the builder is freed with the last view), the views are writable,
+    and a clone's state arrays are private copies."""
+    import gc
+    import tempfile
+    from eqdyna_gb300.case import Case
+    from eqdyna_gb300.configs import config_c0
+    case = Case.from_dir(config_c0(tempfile.mkdtemp(prefix="eqd_view_"), scale=4.0, nsteps=5))
+    assert set(case.build_phases_s) >= {"mesh", "element_tables", "views"}
+    coor = case.arrays["meshCoor"]
+    expect = float(coor.sum())
+    twin = case.clone()
+    twin.arrays["velArr"][:] = 1.0
+    assert not case.arrays["velArr"].any()
+    case.arrays["dispArr"][:3] = 2.0  # writable view
+    del case, twin
+    gc.collect()
+    assert float(coor.sum()) == expect
