@@ -381,6 +381,8 @@ struct Case {
   std::unordered_map<int32_t, int32_t> slave_to_master;
   std::vector<char> station_level;           // (nz): an off-fault station lies at this depth
   double dip_tan = 0.0, dip_norm = 1.0;      // tan(C_degen), (1 + tan^2)^(1/2): the dipping plane
+  std::vector<double> layer_depths;          // material(i, 1), i = 1..nmat (layer bottoms)
+  bool layer_depths_sorted = false;          // strictly increasing: a layer is found by bisection
   std::vector<int32_t> cell_plane_start;     // (nx + 2): first element of each x-layer of cells
   // stations
   std::vector<int32_t> anonfs;               // (3, nOnFound)
@@ -642,6 +644,13 @@ void set_material(Case &c, int e, const double ctr[3]) {
     const double az = std::fabs(ctr[2]);
     if (az < mat_in(in, 1, 1)) {
       m[0] = mat_in(in, 1, 2); m[1] = mat_in(in, 1, 3); m[2] = mat_in(in, 1, 4);
+    } else if (c.layer_depths_sorted) {
+      // the layer i with depth(i-1) <= az < depth(i): the one the loop below selects
+      const auto it = std::upper_bound(c.layer_depths.begin(), c.layer_depths.end(), az);
+      const int i = static_cast<int>(it - c.layer_depths.begin()) + 1;
+      if (i >= 2 && i <= in.nmat) {
+        m[0] = mat_in(in, i, 2); m[1] = mat_in(in, i, 3); m[2] = mat_in(in, i, 4);
+      }
     } else {
       for (int i = 2; i <= in.nmat; ++i) {
         if (az < mat_in(in, i, 1) && az >= mat_in(in, i - 1, 1)) {
@@ -729,6 +738,12 @@ void mesh(Case &c) {
   c.meshCoor.assign(static_cast<size_t>(3) * nxyz, 0.0);
   c.fltrc.assign(static_cast<size_t>(2) * c.nxuni * c.nzuni, 0);
   c.n4yn.assign(in.nOffSt, 0);
+  c.layer_depths.clear();
+  if (in.nmat > 1 && in.n2mat == 4)
+    for (int i = 1; i <= in.nmat; ++i) c.layer_depths.push_back(mat_in(in, i, 1));
+  c.layer_depths_sorted = !c.layer_depths.empty();
+  for (size_t i = 1; i < c.layer_depths.size(); ++i)
+    if (!(c.layer_depths[i] > c.layer_depths[i - 1])) c.layer_depths_sorted = false;
   c.dip_tan = std::tan(in.C_degen / 180.0 * kPi);
   c.dip_norm = std::pow(1.0 + c.dip_tan * c.dip_tan, 0.5);
   c.station_level.assign(c.nz, 0);
