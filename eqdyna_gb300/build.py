@@ -30,7 +30,9 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 HOST_FLAGS = ["-O2", "-fPIC", "-std=c++17", "-ffp-contract=off", "-I" + INCLUDE]
 CU_SOURCES = ["eqd_api.cu", "kernels_elem.cu", "kernels_elem32.cu", "kernels_elem32r.cu",
               "kernels_fault.cu", "kernels_mlp.cu", "noalloc.cu"]
-CU_HEADERS = ["eqd_device.cuh", "eqd_internal.h", "mlp_common.cuh", "elem32_common.cuh"]
+# every header of csrc/ is a dependency of every CUDA translation unit, so that a change to any of
+# them (the Newton loop, the conversions, ...) rebuilds the objects that include it
+CU_HEADERS = sorted(f for f in os.listdir(CSRC) if f.endswith((".cuh", ".h")))
 
 CASE_LIB = os.path.join(LIBDIR, "libeqd_case.so")
 GPU_LIB = os.path.join(LIBDIR, "libeqdyna_gb300.so")

@@ -1826,6 +1826,17 @@ int eqd_gpu_newton_replay(eqd_context *X, int32_t learned, int32_t fast, int64_t
   return EQD_OK;
 }
 
+int eqd_gpu_newton_replay_records(eqd_context *X, int32_t learned, int32_t fast, double *v_host, double *step_host,
+                                  int32_t *flags_host) {
+  if (!X) return EQD_ERR_STATE;
+  Context &c = X->c;
+  cudaSetDevice(c.device);
+  EQD_CUDA_OK(cudaStreamSynchronize(c.stream));
+  long long cc[5] = {0, 0, 0, 0, 0};
+  static_assert(sizeof(int32_t) == sizeof(int), "flags are 32-bit");
+  return newton_replay(c, learned, fast, cc, v_host, step_host, reinterpret_cast<int *>(flags_host));
+}
+
 // ---- ensembles ---------------------------------------------------------------------------------
 struct eqd_ensemble {
   std::vector<eqd_context *> members;

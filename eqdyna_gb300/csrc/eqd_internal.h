@@ -200,6 +200,7 @@ int newton_records(Context &c, double *host, long long cap, long long *count);
 int mlp_train(Context &c, const eqd_mlp_train_options &o, float *epoch_loss, float *holdout_loss);
 int mlp_get(Context &c, float *params, float *norm);
 int mlp_set(Context &c, const float *params, const float *norm);
-int newton_replay(Context &c, int learned, int fast, long long counts[5], double *v_host);
+int newton_replay(Context &c, int learned, int fast, long long counts[5], double *v_host,
+                  double *step_host = nullptr, int *flag_host = nullptr);
 
 }  // namespace eqd

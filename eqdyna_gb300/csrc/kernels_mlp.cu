@@ -298,6 +298,8 @@ template <bool FAST>
 __global__ void __launch_bounds__(128) newton_replay_kernel(const double *__restrict__ rec, long long n,
                                                             int friclaw, double dt, const MlpDevice *m,
                                                             double *__restrict__ v_out,
+                                                            double *__restrict__ step_out,
+                                                            int *__restrict__ flag_out,
                                                             unsigned long long *__restrict__ counts) {
   __shared__ __align__(16) __nv_bfloat16 xs[4][32 * kMlpK1];
   const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -328,6 +330,8 @@ __global__ void __launch_bounds__(128) newton_replay_kernel(const double *__rest
   }
   if (live) {
     if (v_out) v_out[i] = o.v;
+    if (step_out) step_out[i] = o.step;
+    if (flag_out) flag_out[i] = o.iters | o.capped << 8 | (int)fallback << 9 | o.exit_kind << 10;
     warp_count_add(counts + 0, (unsigned)o.iters);
     warp_count_add(counts + 1, (unsigned)o.capped);
     warp_count_add(counts + 2, (unsigned)o.executed);
@@ -552,32 +556,41 @@ int mlp_train(Context &c, const eqd_mlp_train_options &o, float *epoch_loss, flo
   return rc;
 }
 
-int newton_replay(Context &c, int learned, int fast, long long counts[5], double *v_host) {
+int newton_replay(Context &c, int learned, int fast, long long counts[5], double *v_host, double *step_host,
+                  int *flag_host) {
   const long long n = newton_log_count(c);
   if (n <= 0) return EQD_ERR_STATE;
   if (learned && !c.mlp) return EQD_ERR_STATE;
   unsigned long long *dc = nullptr;
-  double *dv = nullptr;
+  double *dv = nullptr, *ds = nullptr;
+  int *df = nullptr;
   MRC(dmalloc(reinterpret_cast<void **>(&dc), 4 * sizeof(unsigned long long)));
   cudaMemset(dc, 0, 4 * sizeof(unsigned long long));
   int rc = EQD_OK;
-  if (v_host && (rc = dmalloc(reinterpret_cast<void **>(&dv), sizeof(double) * n))) {
-    cudaFree(dc);
-    return rc;
+  if (v_host) rc = dmalloc(reinterpret_cast<void **>(&dv), sizeof(double) * n);
+  if (!rc && step_host) rc = dmalloc(reinterpret_cast<void **>(&ds), sizeof(double) * n);
+  if (!rc && flag_host) rc = dmalloc(reinterpret_cast<void **>(&df), sizeof(int) * n);
+  if (!rc) {
+    const unsigned grid = (unsigned)((n + 127) / 128);
+    const MlpDevice *m = learned ? static_cast<const MlpDevice *>(c.mlp) : nullptr;
+    if (fast) newton_replay_kernel<true><<<grid, 128>>>(c.nlog, n, c.sc.friclaw, c.sc.dt, m, dv, ds, df, dc);
+    else newton_replay_kernel<false><<<grid, 128>>>(c.nlog, n, c.sc.friclaw, c.sc.dt, m, dv, ds, df, dc);
+    unsigned long long h[4] = {0, 0, 0, 0};
+    if (cudaMemcpy(h, dc, sizeof(h), cudaMemcpyDeviceToHost) != cudaSuccess) rc = EQD_ERR_CUDA;
+    if (!rc && v_host && cudaMemcpy(v_host, dv, sizeof(double) * n, cudaMemcpyDeviceToHost) != cudaSuccess)
+      rc = EQD_ERR_CUDA;
+    if (!rc && step_host && cudaMemcpy(step_host, ds, sizeof(double) * n, cudaMemcpyDeviceToHost) != cudaSuccess)
+      rc = EQD_ERR_CUDA;
+    if (!rc && flag_host && cudaMemcpy(flag_host, df, sizeof(int) * n, cudaMemcpyDeviceToHost) != cudaSuccess)
+      rc = EQD_ERR_CUDA;
+    for (int k = 0; k < 3; ++k) counts[k] = (long long)h[k];
+    counts[3] = n;
+    counts[4] = (long long)h[3];
   }
-  const unsigned grid = (unsigned)((n + 127) / 128);
-  const MlpDevice *m = learned ? static_cast<const MlpDevice *>(c.mlp) : nullptr;
-  if (fast) newton_replay_kernel<true><<<grid, 128>>>(c.nlog, n, c.sc.friclaw, c.sc.dt, m, dv, dc);
-  else newton_replay_kernel<false><<<grid, 128>>>(c.nlog, n, c.sc.friclaw, c.sc.dt, m, dv, dc);
-  unsigned long long h[4] = {0, 0, 0, 0};
-  if (cudaMemcpy(h, dc, sizeof(h), cudaMemcpyDeviceToHost) != cudaSuccess) rc = EQD_ERR_CUDA;
-  if (!rc && v_host && cudaMemcpy(v_host, dv, sizeof(double) * n, cudaMemcpyDeviceToHost) != cudaSuccess)
-    rc = EQD_ERR_CUDA;
-  for (int k = 0; k < 3; ++k) counts[k] = (long long)h[k];
-  counts[3] = n;
-  counts[4] = (long long)h[3];
   cudaFree(dc);
   if (dv) cudaFree(dv);
+  if (ds) cudaFree(ds);
+  if (df) cudaFree(df);
   return rc;
 }
 

@@ -11,6 +11,11 @@
 // The math is that of the interior element kernel of the time step (one-point hexahedron or
 // degenerated wedge, elastic Hooke update, Kosloff-Frazier stiffness hourglass); it reads the
 // Fortran layout (element-major tables) instead of the step's structure-of-arrays layout.
+//
+// The tables are on the device, where the host cannot look at them before the launch, so the
+// kernel checks every element's node ids (1 .. nnode) and stress offset (0 .. size_stress - 6)
+// itself: an element that fails is skipped (no stress update, no force) and counted in a second
+// file-scope device word, which the call reads back once its work is done.
 #include <mutex>
 
 #include "eqd_device.cuh"
@@ -23,11 +28,14 @@ constexpr int kNoallocBlock = 128;
 constexpr int kMaxDevices = 64;
 
 static __device__ __align__(256) double g_noalloc_force[3 * kNoallocMaxNodes];
+// elements skipped by the last call because of an out-of-range node id or stress offset
+static __device__ int g_noalloc_bad;
 
 std::mutex g_noalloc_mutex;
 double *g_noalloc_ptr[kMaxDevices] = {nullptr};
 
 __global__ void noalloc_clear(double *acc, int n) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) g_noalloc_bad = 0;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) acc[i] = 0.0;
 }
 
@@ -39,8 +47,18 @@ __global__ void __launch_bounds__(kNoallocBlock)
   if (!(et == 1 || et > 10)) return;
   const int nn = v.nnode;
   int n[8];
+  bool ok = true;
 #pragma unroll
-  for (int a = 0; a < 8; ++a) n[a] = v.nodeElemIdRelation[8 * (size_t)e + a] - 1;
+  for (int a = 0; a < 8; ++a) {
+    n[a] = v.nodeElemIdRelation[8 * (size_t)e + a] - 1;
+    ok = ok && n[a] >= 0 && n[a] < nn;
+  }
+  const long long so = v.stressCompIndexArr[e];
+  ok = ok && so >= 0 && so + 6 <= v.size_stress;
+  if (!ok) {  // skipped: contributes nothing, counted for the call to report
+    atomicAdd(&g_noalloc_bad, 1);
+    return;
+  }
   const double *shp = v.eleshp + 24 * (size_t)e;
   const double *phi = v.phi + 32 * (size_t)e;
   double sr[6] = {0, 0, 0, 0, 0, 0};
@@ -70,7 +88,7 @@ __global__ void __launch_bounds__(kNoallocBlock)
   const double cd = lam + 2.0 * mu;
   const double srate[6] = {cd * sr[0] + lam * sr[1] + lam * sr[2], lam * sr[0] + cd * sr[1] + lam * sr[2],
                            lam * sr[0] + lam * sr[1] + cd * sr[2], mu * sr[3], mu * sr[4], mu * sr[5]};
-  double *st = v.stressArr + v.stressCompIndexArr[e];
+  double *st = v.stressArr + so;
   const double tw = -v.eledet[e] * v.w;
   double s6[6];
 #pragma unroll
@@ -136,20 +154,33 @@ int scratch_for_current_device(double **out) {
 extern "C" int eqd_gpu_elem_forces_noalloc(const eqd_elem_device_view *v, double *force_out, void *stream) {
   using namespace eqd;
   if (!v || !force_out) return EQD_ERR_INPUT;
-  if (v->nnode <= 0 || v->nelem < 0) return EQD_ERR_INPUT;
+  if (v->nnode <= 0 || v->nelem < 0 || v->size_stress < 0) return EQD_ERR_INPUT;
   if (v->nnode > kNoallocMaxNodes) return EQD_ERR_INPUT;  // beyond the fixed scratch capacity
   if (!v->nodeElemIdRelation || !v->elemTypeArr || !v->eleshp || !v->eledet || !v->mat || !v->ss ||
       !v->phi || !v->stressArr || !v->stressCompIndexArr || !v->velArr || !v->dispArr)
     return EQD_ERR_INPUT;
+  // the pass is the elastic, stiffness-hourglass form only (src/calcElemKU.f90 with C_elastic = 1,
+  // C_Q = 0; src/hrglss.f90 with C_hg = 1)
+  if (v->C_elastic != 1 || v->C_Q != 0 || v->C_hg != 1) return EQD_ERR_UNSUPPORTED;
+  // an error the caller left pending belongs to the caller: report it, keep it, launch nothing
+  if (cudaPeekAtLastError() != cudaSuccess) return EQD_ERR_CUDA;
   double *acc = nullptr;
   int rc = scratch_for_current_device(&acc);
   if (rc) return rc;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const int n3 = 3 * v->nnode;
   noalloc_clear<<<(n3 + 255) / 256, 256, 0, s>>>(acc, n3);
-  if (v->nelem > 0)
+  if (cudaGetLastError() != cudaSuccess) return EQD_ERR_CUDA;
+  if (v->nelem > 0) {
     noalloc_elem<<<(v->nelem + kNoallocBlock - 1) / kNoallocBlock, kNoallocBlock, 0, s>>>(*v, acc);
+    if (cudaGetLastError() != cudaSuccess) return EQD_ERR_CUDA;
+  }
   noalloc_store<<<(v->nnode + 255) / 256, 256, 0, s>>>(acc, force_out, v->nnode);
   if (cudaGetLastError() != cudaSuccess) return EQD_ERR_CUDA;
-  return EQD_OK;
+  // wait for this call's work and read the count of skipped elements
+  int bad = 0;
+  if (cudaMemcpyFromSymbolAsync(&bad, g_noalloc_bad, sizeof(int), 0, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess)
+    return EQD_ERR_CUDA;
+  return bad ? EQD_ERR_INPUT : EQD_OK;
 }

@@ -24,6 +24,8 @@ struct NewtonOut {
   int iters;     // as the reference counts them (20 when the cap is reached)
   int capped;    // 1 when the 20 iterations ran out without meeting the tolerance
   int executed;  // iterations actually evaluated
+  int exit_kind; // FAST: 0 exit test or cap, 1 fixed point, 2 2-cycle ending on the last
+                 // evaluation, 3 2-cycle ending on the one before it
 };
 
 // Logged solve: NewtonSolve (13 doubles), the plain initial guess, the converged slip rate and
@@ -84,8 +86,9 @@ __device__ __forceinline__ NewtonOut rsf_newton(int friclaw, double dt, const Ne
                                   : 1.0 / (2.0 * p.V0) * exp(s.state0 / p.A);
   double v_eval = v0;                        // FAST: where the law was last evaluated
   double vA = 0.0, thA = 0.0, tcA = 0.0;     // FAST: v_(k-2) and the law evaluated at it
+  double dvA = 0.0;                          // FAST: the Newton step evaluated at v_(k-2)
   double dv_last = 0.0, vt_last = 1.0;       // Newton step and iterate of the last evaluation
-  int iv, executed = 0;
+  int iv, executed = 0, exit_kind = 0;
   for (iv = 1; iv <= 20; ++iv) {
     ++executed;
     double xmu, dxmudv;
@@ -119,16 +122,21 @@ __device__ __forceinline__ NewtonOut rsf_newton(int friclaw, double dt, const Ne
     const double vnew = (vn <= 0.0) ? vt / 2.0 : vn;
     if (FAST && iv < 20) {
       if (vnew == vt) {  // fixed point: v_20 = v_19 = vt
+        exit_kind = 1;
         iv = 21;
         break;
       }
       if (iv >= 2 && vnew == vA) {  // 2-cycle vA, vt, vA, ...
         if ((20 - iv) % 2 == 0) {
           vt = vnew;  // v_20 = vA, v_19 = vt: the evaluation just made
-        } else {      // v_20 = vt, v_19 = vA: the previous evaluation
+          exit_kind = 2;
+        } else {      // v_20 = vt, v_19 = vA: the previous evaluation, step ratio included
           v_eval = vA;
           thTmp = thA;
           taoc_new = tcA;
+          dv_last = dvA;
+          vt_last = vA;
+          exit_kind = 3;
         }
         iv = 21;
         break;
@@ -138,6 +146,7 @@ __device__ __forceinline__ NewtonOut rsf_newton(int friclaw, double dt, const Ne
       vA = vt;
       thA = thTmp;
       tcA = taoc_new;
+      dvA = dv;
     }
     vt = vnew;
   }
@@ -153,6 +162,7 @@ __device__ __forceinline__ NewtonOut rsf_newton(int friclaw, double dt, const Ne
   o.iters = iv > 20 ? 20 : iv;
   o.capped = iv > 20 ? 1 : 0;
   o.executed = executed;
+  o.exit_kind = exit_kind;
   return o;
 }
 

@@ -36,6 +36,17 @@ module eqd_gpu_mod
     integer(c_int32_t) :: use_graph, device, table_layout, block_node, block_fault, sequential_fault
   end type
 
+  ! device addresses of the globalvar arrays for eqd_gpu_elem_forces_noalloc (arrays already on
+  ! the GPU under OpenACC or CUDA Fortran; the call allocates nothing)
+  type, bind(C) :: eqd_elem_device_view
+    integer(c_int32_t) :: nnode, nelem
+    type(c_ptr) :: nodeElemIdRelation, elemTypeArr, eleshp, eledet, mat, ss, phi
+    type(c_ptr) :: stressArr, stressCompIndexArr, velArr, dispArr
+    real(c_double) :: dt, rdampk, w
+    integer(c_int64_t) :: size_stress
+    integer(c_int32_t) :: C_elastic, C_Q, C_hg
+  end type
+
   interface
     integer(c_int) function eqd_gpu_init(s, a, opt, ctx) bind(C, name="eqd_gpu_init")
       import :: c_int, c_ptr, eqd_scalars, eqd_host_arrays, eqd_options
@@ -96,6 +107,12 @@ module eqd_gpu_mod
     integer(c_int) function eqd_host_free(p) bind(C, name="eqd_host_free")
       import :: c_int, c_ptr
       type(c_ptr), value :: p
+    end function
+    integer(c_int) function eqd_gpu_elem_forces_noalloc(view, force_out, stream) &
+        bind(C, name="eqd_gpu_elem_forces_noalloc")
+      import :: c_int, c_ptr, eqd_elem_device_view
+      type(eqd_elem_device_view), intent(in) :: view
+      type(c_ptr), value :: force_out, stream
     end function
   end interface
 

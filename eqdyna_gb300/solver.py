@@ -210,6 +210,22 @@ class GpuSolver:
         out = dict(zip(["iterations", "ivmax_hits", "executed", "records", "fallbacks"], list(counts)))
         return (out, v) if values else out
 
+    def replay_records(self, learned=False, fast=True):
+        """Per logged record of the same replay: converged slip rate, step ratio of the last
+        evaluation, iterations, reached-20, repeated-from-the-plain-guess and (fast loop) how the
+        loop ended (0 exit test or cap, 1 fixed point, 2/3 a 2-cycle)."""
+        n = C.c_int64()
+        self._rc(self.lib.eqd_gpu_newton_records(self._h, None, 0, C.byref(n)), "eqd_gpu_newton_records")
+        v, step = np.zeros(n.value), np.zeros(n.value)
+        flags = np.zeros(n.value, dtype=np.int32)
+        self._rc(self.lib.eqd_gpu_newton_replay_records(self._h, int(bool(learned)), int(bool(fast)),
+                                                        v.ctypes.data_as(N.c_double_p),
+                                                        step.ctypes.data_as(N.c_double_p),
+                                                        flags.ctypes.data_as(C.POINTER(C.c_int32))),
+                 "eqd_gpu_newton_replay_records")
+        return {"v": v, "step": step, "iters": flags & 0xFF, "capped": (flags >> 8) & 1,
+                "fallback": (flags >> 9) & 1, "exit": flags >> 10}
+
     @staticmethod
     def _rc(rc, what):
         if rc != 0:

@@ -278,6 +278,14 @@ int eqd_gpu_mlp_enable(eqd_context *ctx, int32_t on);
  * NULL. */
 int eqd_gpu_newton_replay(eqd_context *ctx, int32_t learned, int32_t fast, int64_t counts[5],
                           double *v_host);
+/* The same replay, per logged record (arrays of the record count; any may be NULL): the converged
+ * slip rate, the step ratio |last Newton step| / |slip rate where it was evaluated| that decides a
+ * repeat from the plain guess, and flags = iterations (as the reference counts them, both runs of
+ * a repeated solve) | reached-20 << 8 | repeated-from-the-plain-guess << 9 | exit << 10, exit (the
+ * fast loop only) 0 exit test or cap, 1 fixed point, 2 and 3 a 2-cycle ending on the last or on
+ * the previous evaluation.  With fast = 0 and fast = 1 every field but the exit must agree. */
+int eqd_gpu_newton_replay_records(eqd_context *ctx, int32_t learned, int32_t fast, double *v_host,
+                                  double *step_host, int32_t *flags_host);
 /* Loss sum((y - t)^2) / (2 n) and its gradient for a model and a batch, computed by the training
  * kernel: x[n][6] normalised inputs, t[n] normalised targets (gradient checks). */
 int eqd_mlp_gradient(int32_t device, const float *params, const float *x, const float *t, int32_t n,
@@ -348,6 +356,8 @@ typedef struct eqd_elem_device_view {
   const int32_t *stressCompIndexArr;  /* (nelem)                                                  */
   const double *velArr, *dispArr;     /* (3, nnode)                                               */
   double dt, rdampk, w;               /* rdampk already multiplied by dt; w = 8                   */
+  int64_t size_stress;                /* length of stressArr (bounds the stress offsets)          */
+  int32_t C_elastic, C_Q, C_hg;       /* the run's switches: only 1, 0, 1 are accepted            */
 } eqd_elem_device_view;
 
 /* Maximum nnode accepted by eqd_gpu_elem_forces_noalloc (size of its fixed scratch). */
@@ -356,14 +366,21 @@ typedef struct eqd_elem_device_view {
 /* Elastic interior-element pass of one step (calcElemKU stress update and forces plus the
  * Kosloff-Frazier hourglass forces, binary64) on the caller's device arrays: updates stressArr in
  * place and overwrites force_out, a DEVICE array (3, nnode), with the per-node sum of the element
- * and hourglass forces.  PML elements (type 2) contribute nothing.  Allocates no device memory:
- * the per-node accumulator is a fixed static device array of EQD_NOALLOC_MAX_NODES nodes
- * (12 MiB, held by every GPU that loads the library until exit); larger meshes are rejected with
- * EQD_ERR_INPUT.  Work is queued on `stream` (a cudaStream_t, NULL = legacy default stream) and
- * the call returns without waiting.  The first call on a device looks up the accumulator's device
- * address with that device current; make that first call before any stream capture.  All calls
- * on a device share the accumulator (it is cleared at the start of each call), so calls whose
- * work overlaps on the GPU race; serialise them on one stream. */
+ * and hourglass forces.  PML elements (type 2) contribute nothing.  Valid only for the elastic
+ * medium without Q and with the stiffness hourglass (C_elastic = 1, C_Q = 0, C_hg = 1); other
+ * switches in the view return EQD_ERR_UNSUPPORTED before any launch.
+ * Allocates no device memory: the per-node accumulator is a fixed static device array of
+ * EQD_NOALLOC_MAX_NODES nodes (12 MiB, held by every GPU that loads the library until exit);
+ * larger meshes are rejected with EQD_ERR_INPUT.  Work is queued on `stream` (a cudaStream_t,
+ * NULL = legacy default stream) and the call waits for it to finish.  The device tables are
+ * checked on the device: an element with a node id outside 1 .. nnode or a stress offset outside
+ * 0 .. size_stress - 6 is skipped (its stress is not updated and it adds no force) and the call
+ * returns EQD_ERR_INPUT after the others have been processed.  A CUDA error already pending when
+ * the call starts is left pending and reported as EQD_ERR_CUDA, with nothing launched.  The first
+ * call on a device looks up the accumulator's device address with that device current; make that
+ * first call before any stream capture.  All calls on a device share the accumulator (it is
+ * cleared at the start of each call), so calls whose work overlaps on the GPU race; serialise
+ * them on one stream. */
 int eqd_gpu_elem_forces_noalloc(const eqd_elem_device_view *view, double *force_out, void *stream);
 
 #ifdef __cplusplus

@@ -1,5 +1,6 @@
 """Ensembles: scenarios of different mesh sizes and time steps advanced together (one launch per
-kernel per step over all members) agree with each member run alone.
+kernel per step over all members) agree with each member run alone, and every member stays within
+the binary32 form's accuracy budget against the binary64 oracle run on that member alone.
 
 Binary32 runs are not bitwise reproducible (the nodal sums end in binary32 L2 reductions from
 several CTAs), so members are compared with their solo runs to relative 1e-4.
@@ -61,6 +62,18 @@ def test_ensemble_matches_members_run_alone():
         both = ta < 1e4
         assert np.all(np.abs(ta[both] - tb[both]) <= c.scalars.dt * 1.000001)
         assert np.abs(fa[:, 75]).max() > 0.0  # the rupture is under way
+    # every batched member against the oracle (the binary32 form's budget: 1 % slip rate, slip and
+    # peak slip rate, rupture time within one step)
+    from conftest import nthreads
+    from oracle import Oracle
+    from test_gpu_fp32 import _check, _errors
+    for c, a in zip(cases, members):
+        cpu = c.clone()
+        Oracle(cpu, nthreads()).step(NSTEPS)
+        err = _errors(cpu, a)
+        print("member", c.sizes["nelem"], "vs oracle", err)
+        assert err["ruptured"] > 0
+        _check(err)
 
 
 def test_ensemble_rejects_streamed_members():

@@ -105,3 +105,23 @@ def test_fp32_learned_form_within_budget(c1_trained):
     print("fp32+learned", err, counts)
     assert counts["learned"] == 300 * case.npair
     _check(err)
+
+
+def test_fast_and_reference_loops_take_the_same_decisions(c1_trained):
+    """Per logged solve, the fault kernel's loop (early stop on a fixed point or a 2-cycle) and the
+    reference's loop give the same slip rate, the same step ratio of the last evaluation (which
+    decides a repeat from the plain guess), the same iteration count, cap and repeat, from the
+    plain and from the learned guess; the early stops of both 2-cycle parities occur in the data."""
+    s, _, _ = c1_trained
+    for learned in (False, True):
+        ref = s.replay_records(learned=learned, fast=False)
+        fast = s.replay_records(learned=learned, fast=True)
+        kinds = np.bincount(fast["exit"], minlength=4)
+        print("learned" if learned else "plain", "exits (test/cap, fixed point, 2-cycle last, 2-cycle previous):",
+              kinds.tolist(), "repeats", int(fast["fallback"].sum()))
+        assert np.array_equal(fast["v"], ref["v"])
+        assert np.array_equal(fast["step"], ref["step"])
+        for k in ("iters", "capped", "fallback"):
+            assert np.array_equal(fast[k], ref[k]), k
+        if not learned:
+            assert kinds[2] > 0 and kinds[3] > 0

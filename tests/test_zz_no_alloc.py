@@ -3,7 +3,10 @@ memory (their arrays are already on the GPU, e.g. under OpenACC or CUDA Fortran 
 or all device memory is planned at start-up).  The entry point keeps its per-node accumulator in
 a fixed static device array, so it must give the same forces and stresses as the time step of the
 context API (eqd_gpu_init / eqd_gpu_step / eqd_gpu_fetch), on two calls in a row: the second call
-must not see anything left in the shared accumulator by the first.
+must not see anything left in the shared accumulator by the first.  The device tables cannot be
+checked on the host, so the kernel checks node ids and stress offsets itself: an element with a
+bad id is skipped and reported (EQD_ERR_INPUT) without a memory fault, the other elements' forces
+are those of the good tables, and the next call with good tables is clean again.
 
 This file is collected last on purpose, and passes both alone in a fresh process and after the
 rest of the suite.
@@ -26,7 +29,8 @@ class ElemDeviceView(C.Structure):
                 ("ss", C.c_void_p), ("phi", C.c_void_p), ("stressArr", C.c_void_p),
                 ("stressCompIndexArr", C.c_void_p), ("velArr", C.c_void_p),
                 ("dispArr", C.c_void_p), ("dt", C.c_double), ("rdampk", C.c_double),
-                ("w", C.c_double)]
+                ("w", C.c_double), ("size_stress", C.c_int64), ("C_elastic", C.c_int32),
+                ("C_Q", C.c_int32), ("C_hg", C.c_int32)]
 
 
 def _rel(a, b):
@@ -69,6 +73,16 @@ def test_noalloc_element_forces_match_the_step_on_two_calls():
     sel = np.where(only)[0]
     interior_stress = (a["stressCompIndexArr"][et != 2][:, None] + np.arange(6)[None, :]).ravel()
 
+    def make_view(d_conn, d_vel, d_disp, **switches):
+        sw = {"C_elastic": 1, "C_Q": 0, "C_hg": 1}
+        sw.update(switches)
+        return ElemDeviceView(nn, ne, d_conn.data_ptr(), d_type.data_ptr(), d_shp.data_ptr(),
+                              d_det.data_ptr(), d_mat.data_ptr(), d_ss.data_ptr(),
+                              d_phi.data_ptr(), d_stress.data_ptr(), d_sidx.data_ptr(),
+                              d_vel.data_ptr(), d_disp.data_ptr(), case.scalars.dt,
+                              case.scalars.rdampk, case.scalars.w, int(a["stressArr"].size),
+                              sw["C_elastic"], sw["C_Q"], sw["C_hg"])
+
     ref = case.clone()
     stream = torch.cuda.current_stream(dev)
     with GpuSolver(ref, use_graph=False) as s:
@@ -77,14 +91,11 @@ def test_noalloc_element_forces_match_the_step_on_two_calls():
         s.fetch()
         d_stress.copy_(t(ref.arrays["stressArr"]))
         for call in range(2):
+            prev_stress = d_stress.cpu().numpy()
             s.step(1)
             s.fetch()
             d_vel, d_disp = t(ref.arrays["velArr"]), t(ref.arrays["dispArr"])
-            view = ElemDeviceView(nn, ne, d_conn.data_ptr(), d_type.data_ptr(), d_shp.data_ptr(),
-                                  d_det.data_ptr(), d_mat.data_ptr(), d_ss.data_ptr(),
-                                  d_phi.data_ptr(), d_stress.data_ptr(), d_sidx.data_ptr(),
-                                  d_vel.data_ptr(), d_disp.data_ptr(), case.scalars.dt,
-                                  case.scalars.rdampk, case.scalars.w)
+            view = make_view(d_conn, d_vel, d_disp)
             rc = lib.eqd_gpu_elem_forces_noalloc(C.byref(view), C.c_void_p(d_force.data_ptr()),
                                                  C.c_void_p(stream.cuda_stream))
             assert rc == 0
@@ -99,7 +110,57 @@ def test_noalloc_element_forces_match_the_step_on_two_calls():
             acc = ref.arrays["nodalForceArr"][eq3[sel] - 1]
             mass = ref.arrays["nodalMassArr"][eq3[sel] - 1]
             assert _rel(force[sel], acc * mass) <= TOL, f"call {call + 1}"
+        good_force = force.copy()
+        good_stress = stress.copy()
+
+        # one interior element with a node id above nnode, another with a 0-based id (0): both are
+        # skipped on the device, the call reports EQD_ERR_INPUT, nothing faults
+        interior = np.where(et != 2)[0]
+        bad = [int(interior[len(interior) // 3]), int(interior[2 * len(interior) // 3])]
+        conn_bad = a["nodeElemIdRelation"].copy().reshape(-1, 8)
+        conn_bad[bad[0], 3] = nn + 5
+        conn_bad[bad[1], 0] = 0
+        d_conn_bad = t(conn_bad.ravel())
+        d_stress.copy_(t(prev_stress))
+        view = make_view(d_conn_bad, d_vel, d_disp)
+        rc = lib.eqd_gpu_elem_forces_noalloc(C.byref(view), C.c_void_p(d_force.data_ptr()),
+                                             C.c_void_p(stream.cuda_stream))
+        assert rc == 1, rc
+        torch.cuda.synchronize(dev)
+        force_bad = d_force.cpu().numpy().reshape(nn, 3)
+        stress_bad = d_stress.cpu().numpy()
+        # the skipped elements kept their stress; every other element was updated as before
+        for e in bad:
+            o = a["stressCompIndexArr"][e]
+            assert np.array_equal(stress_bad[o:o + 6], prev_stress[o:o + 6])
+        keep = np.ones(stress_bad.size, dtype=bool)
+        for e in bad:
+            o = a["stressCompIndexArr"][e]
+            keep[o:o + 6] = False
+        assert np.array_equal(stress_bad[keep & np.isin(np.arange(stress_bad.size), interior_stress)],
+                              good_stress[keep & np.isin(np.arange(stress_bad.size), interior_stress)])
+        # nodes of the skipped elements lost those elements' forces; all others are unchanged
+        touched = np.zeros(nn, dtype=bool)
+        touched[conn[bad].ravel()] = True
+        other = ~touched
+        assert np.isfinite(force_bad).all()
+        assert _rel(force_bad[other], good_force[other]) <= TOL
+
+        # the next call with good tables is clean: the skip count and accumulator start afresh
+        d_stress.copy_(t(prev_stress))
+        view = make_view(d_conn, d_vel, d_disp)
+        rc = lib.eqd_gpu_elem_forces_noalloc(C.byref(view), C.c_void_p(d_force.data_ptr()),
+                                             C.c_void_p(stream.cuda_stream))
+        assert rc == 0
+        torch.cuda.synchronize(dev)
+        assert _rel(d_force.cpu().numpy().reshape(nn, 3)[sel], good_force[sel]) <= TOL
+
+        # switches the pass does not implement are refused before any launch
+        for sw in ({"C_hg": 2}, {"C_elastic": 0}, {"C_Q": 1}):
+            view = make_view(d_conn, d_vel, d_disp, **sw)
+            assert lib.eqd_gpu_elem_forces_noalloc(C.byref(view), C.c_void_p(d_force.data_ptr()),
+                                                   C.c_void_p(stream.cuda_stream)) == 5, sw
 
     # sizes beyond the fixed scratch are refused before any launch
-    big = ElemDeviceView(524289, 1)
+    big = ElemDeviceView(524289, 1, size_stress=0, C_elastic=1, C_Q=0, C_hg=1)
     assert lib.eqd_gpu_elem_forces_noalloc(C.byref(big), C.c_void_p(d_force.data_ptr()), None) == 1
