@@ -60,14 +60,15 @@ REC_ELEM_BYTES = {"interior": 16 + 4 + 48, "pml": 16 + 4 + 120 + 8}
 # (binary64 velocity and displacement, binary32 forces, 1/m and PML split fields, plus the
 # binary32 copies the element kernels gather).
 NODE_BYTES = {"fp64": (152, 536), "fp32": (148, 340)}
-# DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) per element of the binary32
-# kernels on a uniform grid (one record per group), from the ncu capture of C1 at dx = 200 m
-# (profiles/elem_f32_uniform_C1-dx200.md), scaled to a launch by its element count.
-# (the interior pass also reads the 2 KB slot table of each tile, about 18 B per element)
-NCU_TRAFFIC_PER_UNIT = {("elem_interior", "fp32", "records", 1): (132.438272e6 + 16.760320e6) / 1125000,
-                        ("elem_pml", "fp32", "records", 1): (283.675648e6 + 104.746752e6) / 1402000,
-                        # per node of the C1 mesh at dx = 200 m (55 % PML nodes; C1 at 100 m: 56 %)
-                        ("node_update", "fp32", None, None): (299.577856e6 + 298.804992e6) / 2592757}
+# DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) per unit of the binary32 kernels on
+# the full C1 mesh (20,216,000 elements, 20,477,812 nodes; one record per group), from one 1-pass
+# ncu capture of the bench's own launches (profiles/dram_C1_full_fp32.md), scaled to a launch by
+# its unit count.  At full size the node update moves 0.99 of its algorithmic bytes; the element
+# passes 1.31 (PML) and 1.38 (interior): node data gathered again by neighbouring tiles, and the
+# interior pass's 2 KB slot table per tile.
+NCU_TRAFFIC_PER_UNIT = {("elem_interior", "fp32", "records", 1): (1.01e9 + 0.29443e9) / 9000000,
+                        ("elem_pml", "fp32", "records", 1): (2.08e9 + 1.17e9) / 11216000,
+                        ("node_update", "fp32", None, None): (2.38e9 + 2.75e9) / 20477812}
 JOB_STEPS = {"C0": 1000, "C1": 4000, "C2": 6000, "C3": 5000}
 # the result a host program reads after every step: fric rows 71-76 (slip s/d/n, slip rate s/d,
 # peak slip rate) of every fault pair
