@@ -116,6 +116,8 @@ def case_lib():
         lib = _load(_build.CASE_LIB)
         lib.eqd_case_build.argtypes = [C.c_char_p, C.POINTER(C.c_void_p)]
         lib.eqd_case_build.restype = C.c_int
+        lib.eqd_case_build_opt.argtypes = [C.c_char_p, C.c_int32, C.POINTER(C.c_void_p)]
+        lib.eqd_case_build_opt.restype = C.c_int
         lib.eqd_case_view.argtypes = [C.c_void_p, C.POINTER(EqdScalars), C.POINTER(EqdHostArrays)]
         lib.eqd_case_view.restype = C.c_int
         lib.eqd_case_array_len.argtypes = [C.c_void_p, C.c_char_p, C.POINTER(C.c_int32)]
@@ -177,6 +179,8 @@ def gpu_lib():
                      "eqd_gpu_mlp_set", "eqd_gpu_mlp_enable", "eqd_gpu_newton_replay", "eqd_mlp_gradient",
                      "eqd_gpu_newton_replay_records"):
             getattr(lib, name).restype = C.c_int
+        lib.eqd_gpu_element_tables.argtypes = [C.c_int32, C.POINTER(EqdHostArrays), d_p, d_p, d_p, d_p, d_p, d_p, d_p]
+        lib.eqd_gpu_element_tables.restype = C.c_int
         lib.eqd_gpu_check_conversions.argtypes = [C.c_int32, C.c_int64, C.c_uint64, C.POINTER(C.c_int64)]
         lib.eqd_gpu_check_conversions.restype = C.c_int
         lib.eqd_gpu_fetch_fric_rows.argtypes = [C.c_void_p, C.POINTER(C.c_int32), C.c_int32, d_p]
@@ -230,9 +234,9 @@ GPU_SYMBOLS = ["eqd_gpu_init", "eqd_gpu_step", "eqd_gpu_fetch", "eqd_gpu_fetch_f
                "eqd_gpu_init_times",
                "eqd_gpu_newton_log", "eqd_gpu_newton_records", "eqd_gpu_mlp_train", "eqd_gpu_mlp_get",
                "eqd_gpu_mlp_set", "eqd_gpu_mlp_enable", "eqd_gpu_newton_replay", "eqd_mlp_gradient",
-               "eqd_gpu_newton_replay_records",
+               "eqd_gpu_newton_replay_records", "eqd_gpu_element_tables",
                "eqd_gpu_fp64_fma_peak", "eqd_gpu_check_conversions", "eqd_gpu_elem_forces_noalloc"]
-CASE_SYMBOLS = ["eqd_case_build", "eqd_case_view", "eqd_case_array_len", "eqd_case_dims",
+CASE_SYMBOLS = ["eqd_case_build", "eqd_case_build_opt", "eqd_case_view", "eqd_case_array_len", "eqd_case_dims",
                 "eqd_case_lines", "eqd_case_phase_seconds", "eqd_case_free", "eqd_case_last_error"]
 
 

@@ -29,7 +29,10 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 HOST_FLAGS = ["-O2", "-fPIC", "-std=c++17", "-ffp-contract=off", "-I" + INCLUDE]
 CU_SOURCES = ["eqd_api.cu", "kernels_elem.cu", "kernels_elem32.cu", "kernels_elem32r.cu",
-              "kernels_fault.cu", "kernels_mlp.cu", "noalloc.cu"]
+              "kernels_fault.cu", "kernels_mlp.cu", "noalloc.cu", "setup_device.cu"]
+# per-file flags: the device table build restates host arithmetic bit for bit, so nothing in it
+# may be contracted into a fused multiply-add
+CU_FLAGS = {"setup_device.cu": ["--fmad=false"]}
 # every header of csrc/ is a dependency of every CUDA translation unit, so that a change to any of
 # them (the Newton loop, the conversions, ...) rebuilds the objects that include it
 CU_HEADERS = sorted(f for f in os.listdir(CSRC) if f.endswith((".cuh", ".h")))
@@ -55,7 +58,8 @@ def _run(cmd):
 
 def build_case(force=False):
     src = os.path.join(CSRC, "case_builder.cpp")
-    deps = [src, os.path.join(INCLUDE, "eqdyna_case.h"), os.path.join(INCLUDE, "eqdyna_gb300.h")]
+    deps = [src, os.path.join(INCLUDE, "eqdyna_case.h"), os.path.join(INCLUDE, "eqdyna_gb300.h"),
+            os.path.join(CSRC, "eqd_geometry.h")]
     if force or _newer(CASE_LIB, deps):
         os.makedirs(LIBDIR, exist_ok=True)
         _run(["g++", *HOST_FLAGS, "-fopenmp", "-shared", src, "-o", CASE_LIB])
@@ -83,7 +87,7 @@ def build_gpu(force=False, verbose_ptxas=False, jobs=None):
         if force or _newer(obj, [src] + headers):
             cmd = [NVCC, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
                    "-Xcompiler", "-ffp-contract=off", "-Xcompiler", "-fopenmp", "-I" + INCLUDE, "-I" + CSRC,
-                   "-c", src, "-o", obj]
+                   *CU_FLAGS.get(s, []), "-c", src, "-o", obj]
             if verbose_ptxas:
                 cmd += ["-Xptxas", "-v"]
             todo.append(cmd)

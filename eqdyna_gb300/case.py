@@ -148,11 +148,14 @@ class Case:
         self.build_phases_s = None
 
     @classmethod
-    def from_dir(cls, path):
+    def from_dir(cls, path, tables=True):
+        """Build the case in directory `path`.  tables=False builds the mesh only: the per-element
+        tables and nodal masses (eleshp, eledet, elemass, ss, phi, nodalMassArr, fnms) are None,
+        and eqd_gpu_init builds them on the device."""
         lib = N.case_lib()
         h = C.c_void_p()
         t0 = time.perf_counter()
-        rc = lib.eqd_case_build(os.fsencode(path), C.byref(h))
+        rc = lib.eqd_case_build_opt(os.fsencode(path), 0 if tables else 1, C.byref(h))
         if rc != 0:
             raise N.EqdError(rc, "eqd_case_build", lib.eqd_case_last_error().decode())
         owner = _NativeCase(lib, h)

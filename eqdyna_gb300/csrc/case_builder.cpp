@@ -16,6 +16,7 @@
 //                               src/assembleGlobalMass.f90:12-38,283-406, src/library.f90:60-93
 //   initial split-node vel .... src/eqdyna3d.f90:191-212 (init_vel)
 #include "eqdyna_case.h"
+#include "eqd_geometry.h"
 
 #include <algorithm>
 #include <chrono>
@@ -927,28 +928,9 @@ void on_fault_fields(Case &c) {
   }
 }
 
-// src/library.f90:60-93: hexahedron volume (Flanagan & Belytschko 1981 form).
-double hex_volume(const double xl[3][8]) {
-  // it(r, i): node r of the permutation used for node i (src/library.f90:73-76)
-  static const int it[8][8] = {{1, 2, 3, 4, 5, 6, 7, 8}, {2, 3, 4, 1, 6, 7, 8, 5},
-                               {3, 4, 1, 2, 7, 8, 5, 6}, {4, 1, 2, 3, 8, 5, 6, 7},
-                               {5, 8, 7, 6, 1, 4, 3, 2}, {6, 5, 8, 7, 2, 1, 4, 3},
-                               {7, 6, 5, 8, 3, 2, 1, 4}, {8, 7, 6, 5, 4, 3, 2, 1}};
-  double vol = 0.0;
-  for (int i = 0; i < 8; ++i) {
-    auto Y = [&](int r) { return xl[1][it[i][r - 1] - 1]; };
-    auto Z = [&](int r) { return xl[2][it[i][r - 1] - 1]; };
-    const double b = Y(2) * (Z(6) - Z(3) + Z(5) - Z(4)) + Y(3) * (Z(2) - Z(4)) +
-                     Y(4) * (Z(3) - Z(8) + Z(2) - Z(5)) + Y(5) * (Z(8) - Z(6) + Z(4) - Z(2)) +
-                     Y(6) * (Z(5) - Z(2)) + Y(8) * (Z(4) - Z(5));
-    vol += xl[0][i] * b;
-  }
-  return vol / 12.0;
-}
-
-// src/assembleGlobalMass.f90:12-38 with the routines it calls.
+// src/assembleGlobalMass.f90:12-38 with the routines it calls; the per-element math is
+// eqd::geom::element_tables (eqd_geometry.h), shared with the device table build.
 void element_tables(Case &c) {
-  const Inputs &in = c.in;
   const int nelem = static_cast<int>(c.elemTypeArr.size());
   const int nnode = static_cast<int>(c.eqNumStartIndexLoc.size());
   // every entry is written by the element loop below
@@ -959,12 +941,6 @@ void element_tables(Case &c) {
   c.phi.resize(static_cast<size_t>(32) * nelem);
   c.nodalMassArr.assign(std::max(c.equationNumCount, 1), 0.0);
   c.fnms.assign(nnode, 0.0);
-  // one-point local derivatives (src/calcLocalShapeFunc.f90): corner signs
-  static const double sgn[8][3] = {{-1, -1, -1}, {1, -1, -1}, {1, 1, -1}, {-1, 1, -1},
-                                   {-1, -1, 1},  {1, -1, 1},  {1, 1, 1},  {-1, 1, 1}};
-  static const int ha[4][8] = {{1, 1, -1, -1, -1, -1, 1, 1}, {1, -1, -1, 1, -1, 1, 1, -1},
-                               {1, -1, 1, -1, 1, -1, 1, -1}, {-1, 1, -1, 1, 1, -1, 1, -1}};
-  const double w = 8.0;
   // Per-element tables are independent: computed in parallel.  The first element with a
   // non-positive determinant is reported after the loop (an exception cannot leave it).
   int bad = nelem + 1;
@@ -973,94 +949,16 @@ void element_tables(Case &c) {
     double xl[3][8];
     for (int k = 0; k < 8; ++k)
       for (int q = 0; q < 3; ++q) xl[q][k] = coor(c, conn(c, e, k + 1), q + 1);
-    double g[4][8];
-    for (int k = 0; k < 8; ++k) {
-      for (int q = 0; q < 3; ++q) g[q][k] = sgn[k][q] / 8.0;
-      g[3][k] = 1.0 / 8.0;
-    }
-    const int et = c.elemTypeArr[e - 1];
-    if (et == 11 || et == 12) {  // wedge column merge, src/calcGlobalShapeFunc.f90:21-28
-      for (int r = 0; r < 4; ++r) {
-        g[r][2] = g[r][2] + g[r][3];
-        g[r][3] = 0.0;
-        g[r][6] = g[r][6] + g[r][7];
-        g[r][7] = 0.0;
-      }
-    }
-    double xs[3][3];  // xs(j,i) = sum_k g(i,k) xl(j,k)
-    for (int i = 0; i < 3; ++i)
-      for (int j = 0; j < 3; ++j) {
-        double t = 0.0;
-        for (int k = 0; k < 8; ++k) t += g[i][k] * xl[j][k];
-        xs[j][i] = t;
-      }
-    const double c11 = xs[1][1] * xs[2][2] - xs[1][2] * xs[2][1];
-    const double c12 = xs[1][2] * xs[2][0] - xs[1][0] * xs[2][2];
-    const double c13 = xs[1][0] * xs[2][1] - xs[1][1] * xs[2][0];
-    const double c21 = xs[2][1] * xs[0][2] - xs[2][2] * xs[0][1];
-    const double c22 = xs[2][2] * xs[0][0] - xs[2][0] * xs[0][2];
-    const double c23 = xs[2][0] * xs[0][1] - xs[2][1] * xs[0][0];
-    const double c31 = xs[0][1] * xs[1][2] - xs[0][2] * xs[1][1];
-    const double c32 = xs[0][2] * xs[1][0] - xs[0][0] * xs[1][2];
-    const double c33 = xs[0][0] * xs[1][1] - xs[0][1] * xs[1][0];
-    const double det = xs[0][0] * c11 + xs[0][1] * c12 + xs[0][2] * c13;
-    if (!(det > 0.0)) {
+    const size_t eo = static_cast<size_t>(e - 1);
+    double em[8], det = 0.0;
+    if (!eqd::geom::element_tables(xl, c.elemTypeArr[e - 1], &c.matRows[5 * eo], &c.eleshp[24 * eo], det, em,
+                                   &c.ss[6 * eo], &c.phi[32 * eo])) {
       bad = std::min(bad, e);
       continue;
     }
-    double gs[4][8];
-    for (int k = 0; k < 8; ++k) {
-      gs[0][k] = (g[0][k] * c11 + g[1][k] * c12 + g[2][k] * c13) / det;
-      gs[1][k] = (g[0][k] * c21 + g[1][k] * c22 + g[2][k] * c23) / det;
-      gs[2][k] = (g[0][k] * c31 + g[1][k] * c32 + g[2][k] * c33) / det;
-      gs[3][k] = g[3][k];
-    }
-    // returned xs = cofactor matrix / det, column-major reshape of (c11,c12,c13,c21,...)
-    double xi[3][3] = {{c11 / det, c21 / det, c31 / det},
-                       {c12 / det, c22 / det, c32 / det},
-                       {c13 / det, c23 / det, c33 / det}};
-    // lumped mass, src/assembleGlobalMass.f90:376-406
-    const double *m = &c.matRows[5 * static_cast<size_t>(e - 1)];
-    const double totmas = m[2] * w * det;
-    double work[8], dsum = 0.0;
-    for (int k = 0; k < 8; ++k) {
-      const double t2 = totmas * gs[3][k] * gs[3][k];
-      dsum += t2;
-      work[k] = t2;
-    }
-    const double t1 = totmas / dsum;
-    double *em = &c.elemass[24 * static_cast<size_t>(e - 1)];
-    for (int k = 0; k < 8; ++k)
-      for (int q = 0; q < 3; ++q) em[3 * k + q] = t1 * work[k];
     c.eledet[e - 1] = det;
     for (int k = 0; k < 8; ++k)
-      for (int q = 0; q < 3; ++q) c.eleshp[24 * static_cast<size_t>(e - 1) + 3 * k + q] = gs[q][k];
-    // hourglass tables, src/assembleGlobalMass.f90:328-374
-    const double vol = hex_volume(xl);
-    double ce = m[4] * (3 * m[3] + 2 * m[4]) / (m[3] + m[4]);
-    ce = 16.0 * ce / 15.0;
-    const double co = ce * vol / 48.0;
-    double *s = &c.ss[6 * static_cast<size_t>(e - 1)];
-    s[0] = co * (xi[0][0] * xi[0][0] + xi[1][0] * xi[1][0] + xi[2][0] * xi[2][0]);
-    s[1] = co * (xi[0][0] * xi[0][1] + xi[1][0] * xi[1][1] + xi[2][0] * xi[2][1]);
-    s[2] = co * (xi[0][0] * xi[0][2] + xi[1][0] * xi[1][2] + xi[2][0] * xi[2][2]);
-    s[3] = co * (xi[0][1] * xi[0][1] + xi[1][1] * xi[1][1] + xi[2][1] * xi[2][1]);
-    s[4] = co * (xi[0][1] * xi[0][2] + xi[1][1] * xi[1][2] + xi[2][1] * xi[2][2]);
-    s[5] = co * (xi[0][2] * xi[0][2] + xi[1][2] * xi[1][2] + xi[2][2] * xi[2][2]);
-    double *ph = &c.phi[32 * static_cast<size_t>(e - 1)];
-    for (int mode = 0; mode < 4; ++mode) {
-      double pm[8];
-      for (int j = 0; j < 8; ++j) {
-        double t = 0.0;
-        for (int k = 0; k < 8; ++k)
-          t += ha[mode][k] * (xl[0][k] * gs[0][j] + xl[1][k] * gs[1][j] + xl[2][k] * gs[2][j]);
-        pm[j] = ha[mode][j] - t;
-      }
-      double nrm = 0.0;
-      for (int j = 0; j < 8; ++j) nrm += pm[j] * pm[j];
-      nrm = std::sqrt(nrm / 8.0);
-      for (int j = 0; j < 8; ++j) ph[8 * mode + j] = pm[j] / nrm;
-    }
+      for (int q = 0; q < 3; ++q) c.elemass[24 * eo + 3 * k + q] = em[k];
   }
   if (bad <= nelem) fail("non-positive determinant at element " + std::to_string(bad));
   // nodal mass, src/assembleGlobalMass.f90:283-326.  The reference adds the element masses
@@ -1106,6 +1004,16 @@ void element_tables(Case &c) {
   }
   if (fixed_dof) fail("3-DOF node with a fixed DOF is not supported");
   // wedge sanity check, src/assembleGlobalMass.f90:43-55
+  for (int e = 1; e <= nelem; ++e) {
+    const int et = c.elemTypeArr[e - 1];
+    if (et >= 11 && et <= 12 && conn(c, e, 3) != conn(c, e, 4)) fail("wrongly created wedge");
+  }
+}
+
+// The checks of element_tables that do not need the tables (a mesh-only build): wedge sanity,
+// src/assembleGlobalMass.f90:43-55.
+void mesh_checks(Case &c) {
+  const int nelem = static_cast<int>(c.elemTypeArr.size());
   for (int e = 1; e <= nelem; ++e) {
     const int et = c.elemTypeArr[e - 1];
     if (et >= 11 && et <= 12 && conn(c, e, 3) != conn(c, e, 4)) fail("wrongly created wedge");
@@ -1209,7 +1117,9 @@ extern "C" {
 
 const char *eqd_case_last_error(void) { return g_case_error.c_str(); }
 
-int eqd_case_build(const char *dir, eqd_case **out) {
+int eqd_case_build(const char *dir, eqd_case **out) { return eqd_case_build_opt(dir, 0, out); }
+
+int eqd_case_build_opt(const char *dir, int32_t flags, eqd_case **out) {
   if (!dir || !out) return EQD_ERR_INPUT;
   *out = nullptr;
   auto *h = new eqd_case();
@@ -1226,7 +1136,8 @@ int eqd_case_build(const char *dir, eqd_case **out) {
     lap(1);
     on_fault_fields(h->c);
     lap(2);
-    element_tables(h->c);
+    if (flags & EQD_CASE_MESH_ONLY) mesh_checks(h->c);
+    else element_tables(h->c);
     lap(3);
     finish(h->c);
     lap(4);
@@ -1260,18 +1171,18 @@ int eqd_case_view(eqd_case *h, eqd_scalars *s, eqd_host_arrays *a) {
   a->eqNumStartIndexLoc = c.eqNumStartIndexLoc.data();
   a->numOfDofPerNodeArr = c.numOfDofPerNodeArr.data();
   a->meshCoor = c.meshCoor.data();
-  a->eleshp = c.eleshp.data();
-  a->eledet = c.eledet.data();
+  a->eleshp = c.eleshp.empty() ? nullptr : c.eleshp.data();
+  a->eledet = c.eledet.empty() ? nullptr : c.eledet.data();
   a->mat = c.mat.data();
-  a->elemass = c.elemass.data();
-  a->ss = c.ss.data();
-  a->phi = c.phi.data();
+  a->elemass = c.elemass.empty() ? nullptr : c.elemass.data();
+  a->ss = c.ss.empty() ? nullptr : c.ss.data();
+  a->phi = c.phi.empty() ? nullptr : c.phi.data();
   a->stressArr = c.stressArr.data();
   a->stressCompIndexArr = c.stressCompIndexArr.data();
   a->pstrain = c.pstrain.data();
   a->eleporep = c.eleporep.data();
-  a->nodalMassArr = c.nodalMassArr.data();
-  a->fnms = c.fnms.data();
+  a->nodalMassArr = c.nodalMassArr.empty() ? nullptr : c.nodalMassArr.data();
+  a->fnms = c.fnms.empty() ? nullptr : c.fnms.data();
   a->v1 = c.v1.data();
   a->velArr = c.velArr.data();
   a->dispArr = c.dispArr.data();

@@ -29,6 +29,17 @@ __device__ __forceinline__ void kahan_add(float &s, float &c, float x) {
   s = t;
 }
 
+// Kahan step on two independent sums at once with the packed binary32 pair instructions of sm_100
+// and later (__fadd2_rn / __ffma2_rn: two lanes per issued instruction, each lane rounded as the
+// scalar operation).  fma(a, -1, b) is b - a rounded once, so every lane is bit for bit kahan_add.
+__device__ __forceinline__ void kahan_add2(float2 &s, float2 &c, float2 x) {
+  const float2 m1 = make_float2(-1.f, -1.f);
+  const float2 y = __ffma2_rn(c, m1, x);                // x - c
+  const float2 t = __fadd2_rn(s, y);                    // s + y
+  c = __ffma2_rn(y, m1, __ffma2_rn(s, m1, t));          // (t - s) - y
+  s = t;
+}
+
 __device__ __forceinline__ float viscous_pattern_f(int m, int a) {
   const unsigned neg[4] = {0x3Cu, 0x96u, 0xAAu, 0x5Au};
   return ((neg[m] >> a) & 1u) ? -1.0f : 1.0f;
@@ -342,7 +353,7 @@ __device__ __forceinline__ void interior_element(const Src &S, const float *sv, 
 }
 
 // Interior gather: one thread per tile node, Kahan-compensated sums of its incidences in a fixed
-// order, one binary32 L2 reduction per component.
+// order, one binary32 L2 reduction per component.  The x and y sums run as one packed pair.
 __device__ __forceinline__ void interior_gather(const ElemGroup<float> &g, int M, int nb,
                                                 const unsigned short *incp, const unsigned short *sinc,
                                                 const float *fs, float *__restrict__ F, int nnode,
@@ -350,16 +361,18 @@ __device__ __forceinline__ void interior_gather(const ElemGroup<float> &g, int M
   for (int j = threadIdx.x; j < M; j += blockDim.x) {
     // the node id is loaded first: its latency runs under the sums
     const int n = sids ? sids[j] : __ldg(g.tile_nodes + nb + j);
-    float hi[3] = {0.f, 0.f, 0.f}, lo[3] = {0.f, 0.f, 0.f};
+    float2 hxy = make_float2(0.f, 0.f), lxy = make_float2(0.f, 0.f);
+    float hz = 0.f, lz = 0.f;
     const int q1 = incp[j + 1];
     for (int q = incp[j]; q < q1; ++q) {
       const int r = sinc[q];  // corner * kTile + local element
       const int a = r / kTile, el = r - a * kTile;
-#pragma unroll
-      for (int c = 0; c < 3; ++c) kahan_add(hi[c], lo[c], fs[(c * 8 + a) * kTile + el]);
+      kahan_add2(hxy, lxy, make_float2(fs[(0 * 8 + a) * kTile + el], fs[(1 * 8 + a) * kTile + el]));
+      kahan_add(hz, lz, fs[(2 * 8 + a) * kTile + el]);
     }
-#pragma unroll
-    for (int c = 0; c < 3; ++c) atomicAdd(F + (size_t)c * nnode + n, hi[c] - lo[c]);
+    atomicAdd(F + n, hxy.x - lxy.x);
+    atomicAdd(F + (size_t)nnode + n, hxy.y - lxy.y);
+    atomicAdd(F + 2 * (size_t)nnode + n, hz - lz);
   }
 }
 
@@ -473,36 +486,42 @@ __device__ __forceinline__ void pml_element(const Src &S, const float *sv, const
 }
 
 // PML gather: one thread per tile node; the split-field forces of an incidence are rebuilt from
-// the element's det * shape gradient of the corner (w_of(el, a, wx, wy, wz) for local element el,
-// corner a: the binary32 products dw * shp, as in pml_element) and its split-stress sums.
+// the element's det * shape gradient of the corner and its split-stress sums.  w2_of(el, a, wxx,
+// wyy, wzz, wxy) gives the negated binary32 products -dw * shp of corner a of local element el as
+// the pairs (wx, wx), (wy, wy), (wz, wz), (wx, wy) (as in pml_element).  The nine split components
+// run as four packed pairs, (0, 3) = wx (sxx, sxy), (1, 4) = wy (sxy, syy), (2, 5) = wz (sxz, syz),
+// (6, 7) = (wx, wy) (sxz, syz), and a single 8 = wz szz; the hourglass forces as (x, y) and z.
 // 12-DOF nodes reduce 9 split components + 3 into F9 / F; 3-DOF nodes on the PML boundary take
 // the compensated sum of their 4 partials.
-template <class WOf>
+template <class W2Of>
 __device__ __forceinline__ void pml_gather(const ElemGroup<float> &g, int M, int nb, const unsigned short *incp,
                                            const unsigned short *sinc, const float *es, const float *cfh,
-                                           const WOf &w_of, float *__restrict__ F, float *__restrict__ F9,
+                                           const W2Of &w2_of, float *__restrict__ F, float *__restrict__ F9,
                                            int nnode, int n_int, int npml, const int *sids) {
   for (int j = threadIdx.x; j < M; j += blockDim.x) {
     // the node id is loaded first: its latency runs under the sums
     const int n = sids ? sids[j] : __ldg(g.tile_nodes + nb + j);
-    float hi[12], lo[12];
-#pragma unroll
-    for (int q = 0; q < 12; ++q) hi[q] = lo[q] = 0.f;
+    const float2 z2 = make_float2(0.f, 0.f);
+    float2 h03 = z2, l03 = z2, h14 = z2, l14 = z2, h25 = z2, l25 = z2, h67 = z2, l67 = z2, hf = z2, lf = z2;
+    float h8 = 0.f, l8 = 0.f, hfz = 0.f, lfz = 0.f;
     const int q1 = incp[j + 1];
     for (int q = incp[j]; q < q1; ++q) {
       const int r = sinc[q];
       const int a = r / kTile, el = r - a * kTile;
-      float wx, wy, wz;
-      w_of(el, a, wx, wy, wz);
+      float2 wxx, wyy, wzz, wxy;
+      w2_of(el, a, wxx, wyy, wzz, wxy);
       const float sxx = es[el], syy = es[kTile + el], szz = es[2 * kTile + el];
       const float sxy = es[3 * kTile + el], sxz = es[4 * kTile + el], syz = es[5 * kTile + el];
-      const float f9[9] = {-wx * sxx, -wy * sxy, -wz * sxz, -wx * sxy, -wy * syy,
-                           -wz * syz, -wx * sxz, -wy * syz, -wz * szz};
-#pragma unroll
-      for (int i = 0; i < 9; ++i) kahan_add(hi[i], lo[i], f9[i]);
-#pragma unroll
-      for (int c = 0; c < 3; ++c) kahan_add(hi[9 + c], lo[9 + c], cfh[(c * 8 + a) * kTile + el]);
+      kahan_add2(h03, l03, __fmul2_rn(wxx, make_float2(sxx, sxy)));
+      kahan_add2(h14, l14, __fmul2_rn(wyy, make_float2(sxy, syy)));
+      kahan_add2(h25, l25, __fmul2_rn(wzz, make_float2(sxz, syz)));
+      kahan_add2(h67, l67, __fmul2_rn(wxy, make_float2(sxz, syz)));
+      kahan_add(h8, l8, wzz.x * szz);
+      kahan_add2(hf, lf, make_float2(cfh[(0 * 8 + a) * kTile + el], cfh[(1 * 8 + a) * kTile + el]));
+      kahan_add(hfz, lfz, cfh[(2 * 8 + a) * kTile + el]);
     }
+    const float hi[12] = {h03.x, h14.x, h25.x, h03.y, h14.y, h25.y, h67.x, h67.y, h8, hf.x, hf.y, hfz};
+    const float lo[12] = {l03.x, l14.x, l25.x, l03.y, l14.y, l25.y, l67.x, l67.y, l8, lf.x, lf.y, lfz};
     if (n >= n_int) {
       const int slot = n - n_int;
 #pragma unroll
@@ -523,17 +542,21 @@ __device__ __forceinline__ void pml_gather(const ElemGroup<float> &g, int M, int
   }
 }
 
-// w_of for table sources: dw * shape gradient of corner a of the element that src_of(el) reads.
+// w2_of for table sources: the negated products -dw * shape gradient of corner a of the element
+// that src_of(el) reads, as the pairs pml_gather takes.
 template <int HG, class SrcOf>
 struct WFromSrc {
   SrcOf src_of;
-  __device__ void operator()(int el, int a, float &wx, float &wy, float &wz) const {
+  __device__ void operator()(int el, int a, float2 &wxx, float2 &wyy, float2 &wzz, float2 &wxy) const {
     using C = TabCommon<HG>;
     const auto S = src_of(el);
     const float dw = S.g(C::DET);
-    wx = dw * S.g(C::SHP + 3 * a);
-    wy = dw * S.g(C::SHP + 3 * a + 1);
-    wz = dw * S.g(C::SHP + 3 * a + 2);
+    const float wx = -(dw * S.g(C::SHP + 3 * a)), wy = -(dw * S.g(C::SHP + 3 * a + 1));
+    const float wz = -(dw * S.g(C::SHP + 3 * a + 2));
+    wxx = make_float2(wx, wx);
+    wyy = make_float2(wy, wy);
+    wzz = make_float2(wz, wz);
+    wxy = make_float2(wx, wy);
   }
 };
 template <int HG, class SrcOf>

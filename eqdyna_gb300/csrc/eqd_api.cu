@@ -10,11 +10,13 @@
 #include "eqd_device.cuh"
 #include "elem32_common.cuh"
 #include "mlp_common.cuh"
+#include "setup_device.h"
 
 #include <omp.h>
 #include <parallel/algorithm>
 
 #include <algorithm>
+#include <memory>
 #include <chrono>
 #include <tuple>
 #include <unordered_map>
@@ -490,10 +492,13 @@ int validate(const eqd_scalars *s, const eqd_host_arrays *a) {
   if (!s || !a) return EQD_ERR_INPUT;
   if (a->nnode <= 0 || a->nelem <= 0 || a->neq <= 0) return EQD_ERR_INPUT;
   if (!a->nodeElemIdRelation || !a->elemTypeArr || !a->eqNumIndexArr || !a->eqNumStartIndexLoc ||
-      !a->numOfDofPerNodeArr || !a->meshCoor || !a->eleshp || !a->eledet || !a->mat || !a->ss ||
-      !a->phi || !a->stressArr || !a->stressCompIndexArr || !a->nodalMassArr || !a->fnms ||
+      !a->numOfDofPerNodeArr || !a->meshCoor || !a->mat || !a->stressArr || !a->stressCompIndexArr ||
       !a->v1 || !a->velArr || !a->dispArr || !a->nodalForceArr)
     return EQD_ERR_INPUT;
+  // the per-element tables and nodal masses: all given, or none (then built on the device)
+  const int given = !!a->eleshp + !!a->eledet + !!a->ss + !!a->phi + !!a->nodalMassArr + !!a->fnms;
+  if (given != 0 && given != 6) return EQD_ERR_INPUT;
+  if (given == 0 && a->elemass) return EQD_ERR_INPUT;
   if (s->dt <= 0.0 || s->nstep < 0) return EQD_ERR_INPUT;
   if (s->C_hg != 1 && s->C_hg != 2) return EQD_ERR_UNSUPPORTED;
   if (a->ntotft != 1 && a->ntotft != 0) return EQD_ERR_UNSUPPORTED;
@@ -502,6 +507,48 @@ int validate(const eqd_scalars *s, const eqd_host_arrays *a) {
   if (s->C_Q == 1 && s->C_elastic == 0) return EQD_ERR_UNSUPPORTED;
   if (s->C_Q < 0 || s->C_Q > 2) return EQD_ERR_INPUT;
   return EQD_OK;
+}
+
+// Tables of a group's elements (ids, -1 for an empty slot) computed on the device from the mesh
+// and copied into the group's host rows (shp[q * m + i] ...), in chunks of device scratch.
+template <class V>
+int group_tables_from_device(const DeviceMesh &dm, const std::vector<int> &ids, int m, double w, V &shp, V &phi,
+                             V &ss, V &detw, std::vector<double> *em) {
+  if (m <= 0) return EQD_OK;
+  const int cn = std::min(m, 1 << 22);
+  double *d = nullptr;
+  int *did = nullptr;
+  const size_t rows = 24 + 32 + 6 + 1 + 8;
+  if (cudaMalloc(&d, rows * cn * sizeof(double)) != cudaSuccess || cudaMalloc(&did, cn * sizeof(int)) != cudaSuccess) {
+    cudaGetLastError();
+    if (d) cudaFree(d);
+    return EQD_ERR_OOM;
+  }
+  int rc = EQD_OK;
+  double *dshp = d, *dphi = d + 24 * (size_t)cn, *dss = dphi + 32 * (size_t)cn, *ddet = dss + 6 * (size_t)cn;
+  double *dem = ddet + cn;
+  for (int i0 = 0; i0 < m && !rc; i0 += cn) {
+    const int n = std::min(cn, m - i0);
+    if (cudaMemcpy(did, ids.data() + i0, n * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess) {
+      rc = EQD_ERR_CUDA;
+      break;
+    }
+    if ((rc = device_group_tables(dm, did, n, cn, w, dshp, ddet, em ? dem : nullptr, dss, dphi, 0))) break;
+    auto get = [&](double *dst, const double *src, int nrows) {
+      for (int q = 0; q < nrows && !rc; ++q)
+        if (cudaMemcpy(dst + (size_t)q * m + i0, src + (size_t)q * cn, n * sizeof(double), cudaMemcpyDeviceToHost) !=
+            cudaSuccess)
+          rc = EQD_ERR_CUDA;
+    };
+    get(shp.data(), dshp, 24);
+    get(phi.data(), dphi, 32);
+    get(ss.data(), dss, 6);
+    get(detw.data(), ddet, 1);
+    if (em) get(em->data(), dem, 8);
+  }
+  cudaFree(d);
+  cudaFree(did);
+  return rc;
 }
 
 int build_device_state(eqd_context &X, const eqd_scalars &s, const eqd_host_arrays &a) {
@@ -524,6 +571,21 @@ int build_device_state(eqd_context &X, const eqd_scalars &s, const eqd_host_arra
     if (loc < 1 || loc > a.size_eqidx) return -2;
     return a.eqNumIndexArr[loc - 1];
   };
+  // Without host tables the element tables and nodal masses are built on the device from the mesh
+  // (setup_device.cu), bit for bit the host's: a node's mass is the value of each of its equations
+  // in nodalMassArr and its fnms.
+  const bool dev_tables = a.eleshp == nullptr;
+  std::unique_ptr<DeviceMesh> dmesh;
+  std::vector<double> dev_mass;
+  if (dev_tables) {
+    for (long long q = 0; q < 8 * (long long)ne; ++q)
+      if (a.nodeElemIdRelation[q] < 1 || a.nodeElemIdRelation[q] > nn) return EQD_ERR_INPUT;
+    dmesh.reset(new DeviceMesh());
+    RC(dmesh->upload(a));
+    RC(device_nodal_mass(a, *dmesh, dev_mass));
+  }
+  auto eq_mass = [&](int node, int e) { return dev_tables ? dev_mass[node - 1] : a.nodalMassArr[e - 1]; };
+  auto node_fnms = [&](int node) { return dev_tables ? dev_mass[node - 1] : a.fnms[node - 1]; };
   // ---- nodes ----
   X.node_dev.assign(nn, -1);
   X.node_orig.clear();
@@ -551,7 +613,7 @@ int build_device_state(eqd_context &X, const eqd_scalars &s, const eqd_host_arra
         for (int k = 1; k <= 3; ++k) {
           const int e = eq(node, k);
           if (e < 1 || e > a.neq) return EQD_ERR_UNSUPPORTED;  // fixed 3-DOF node: not built
-          const double mk = a.nodalMassArr[e - 1];
+          const double mk = eq_mass(node, e);
           if (k == 1) m = mk;
           else if (mk != m) return EQD_ERR_UNSUPPORTED;  // anisotropic lumped mass: not built
           vel[(k - 1) * (size_t)nn + d] = a.v1[e - 1];
@@ -564,12 +626,12 @@ int build_device_state(eqd_context &X, const eqd_scalars &s, const eqd_host_arra
         for (int k = 0; k < 3; ++k) vel[k * (size_t)nn + d] = a.velArr[3 * (size_t)j + k];
         const int e1 = eq(node, 1);
         if (e1 > 0) {
-          const double m = a.nodalMassArr[e1 - 1];
+          const double m = eq_mass(node, e1);
           if (!(m > 0)) return EQD_ERR_INPUT;
           for (int k = 1; k <= 12; ++k) {
             const int e = eq(node, k);
             if (e < 1 || e > a.neq) return EQD_ERR_UNSUPPORTED;
-            if (a.nodalMassArr[e - 1] != m) return EQD_ERR_UNSUPPORTED;
+            if (eq_mass(node, e) != m) return EQD_ERR_UNSUPPORTED;
             if (k <= 9) {
               v9[(k - 1) * (size_t)np_ + p] = a.v1[e - 1];
               F9[(k - 1) * (size_t)np_ + p] = a.nodalForceArr[e - 1];
@@ -700,10 +762,12 @@ int build_device_state(eqd_context &X, const eqd_scalars &s, const eqd_host_arra
           for (int k = 0; k < 3; ++k) ctr[k] += a.meshCoor[3 * (size_t)(node - 1) + k];
         }
         for (double &v : ctr) v /= 8.0;
-        for (int q = 0; q < 24; ++q) shp[q * (size_t)m + i] = a.eleshp[24 * (size_t)e + q];
-        for (int q = 0; q < 32; ++q) phi[q * (size_t)m + i] = a.phi[32 * (size_t)e + q];
-        for (int q = 0; q < 6; ++q) ss[q * (size_t)m + i] = a.ss[6 * (size_t)e + q];
-        detw[i] = a.eledet[e] * s.w;
+        if (!dev_tables) {  // (else filled from the device below)
+          for (int q = 0; q < 24; ++q) shp[q * (size_t)m + i] = a.eleshp[24 * (size_t)e + q];
+          for (int q = 0; q < 32; ++q) phi[q * (size_t)m + i] = a.phi[32 * (size_t)e + q];
+          for (int q = 0; q < 6; ++q) ss[q * (size_t)m + i] = a.ss[6 * (size_t)e + q];
+          detw[i] = a.eledet[e] * s.w;
+        }
         lam[i] = a.mat[3 * (size_t)ne + e];
         mu[i] = a.mat[4 * (size_t)ne + e];
         const int64_t base = a.stressCompIndexArr[e];
@@ -721,7 +785,7 @@ int build_device_state(eqd_context &X, const eqd_scalars &s, const eqd_host_arra
             pab[(3 + k) * (size_t)m + i] = 1.0 / (1.0 / s.dt + dm[k] / 2.0);
           }
         }
-        if (body) {
+        if (body && !dev_tables) {
           if (!a.elemass) return EQD_ERR_INPUT;
           for (int q = 0; q < 8; ++q) {
             const double m0 = a.elemass[24 * (size_t)e + 3 * q];
@@ -730,7 +794,7 @@ int build_device_state(eqd_context &X, const eqd_scalars &s, const eqd_host_arra
             em[q * (size_t)m + i] = m0;
           }
         }
-        if (s.C_hg == 2)
+        if (s.C_hg == 2 && !dev_tables)
           hg[i] = 0.25 * s.kapa_hg * a.mat[2 * (size_t)ne + e] * a.mat[e] * std::pow(a.eledet[e] * s.w, 2.0 / 3.0);
         if (grp == 0 && s.C_elastic == 0) {
           porep[i] = a.eleporep ? a.eleporep[e] : 0.0;
@@ -763,6 +827,15 @@ int build_device_state(eqd_context &X, const eqd_scalars &s, const eqd_host_arra
       }
     }
     if (bad_) return bad_;
+    if (dev_tables) {
+      RC(group_tables_from_device(*dmesh, ids, m, s.w, shp, phi, ss, detw, body ? &em : nullptr));
+      if (s.C_hg == 2) {
+#pragma omp parallel for schedule(static)
+        for (int i = 0; i < m; ++i)
+          if (ids[i] >= 0)
+            hg[i] = 0.25 * s.kapa_hg * a.mat[2 * (size_t)ne + ids[i]] * a.mat[ids[i]] * std::pow(detw[i], 2.0 / 3.0);
+      }
+    }
     any_s0 = s0_any;
     if (c.fp32 && grp == 1 && !X.split_node.empty()) {  // does a PML element touch a split node?
       int touch = 0;
@@ -964,8 +1037,8 @@ int build_device_state(eqd_context &X, const eqd_scalars &s, const eqd_host_arra
         geo[(6 + k) * (size_t)npair + i] = a.ud[3 * (size_t)i + k];
       }
       geo[9 * (size_t)npair + i] = a.arn[i];
-      geo[10 * (size_t)npair + i] = a.fnms[sl - 1];
-      geo[11 * (size_t)npair + i] = a.fnms[ms - 1];
+      geo[10 * (size_t)npair + i] = node_fnms(sl);
+      geo[11 * (size_t)npair + i] = node_fnms(ms);
       const double *x = a.meshCoor + 3 * (size_t)(sl - 1);
       geo[12 * (size_t)npair + i] = std::sqrt((x[0] - s.xsource) * (x[0] - s.xsource) +
                                               (x[1] - s.ysource) * (x[1] - s.ysource) +

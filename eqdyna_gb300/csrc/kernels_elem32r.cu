@@ -182,7 +182,9 @@ __device__ __forceinline__ void pml_rec_body(const ElemArgs32 &a, int tile) {
   using C = TabCommon<HG>;
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) unsigned long long bar;
-  __shared__ float cw[24];  // UNI: det * shape gradient (3 a + k) of the group's record
+  // UNI: per corner a the negated det * shape gradient of the group's record as the pairs of
+  // pml_gather: (wx, wx), (wy, wy), (wz, wz), (wx, wy)
+  __shared__ __align__(16) float cw2[8][8];
   const ElemGroup<float> &g = a.g;
   const int Mmax = g.max_tile_nodes;
   float *tab = reinterpret_cast<float *>(smem);
@@ -202,7 +204,11 @@ __device__ __forceinline__ void pml_rec_body(const ElemArgs32 &a, int tile) {
     copy_rows(tab, L::RID, g.rec_id, 1, ld, e0, &bar);
     copy_rows(tab, L::ABID, g.ab_id, 2, ld, e0, &bar);
   }
-  if (UNI && tid < 24) cw[tid] = a.rp.v[C::DET] * a.rp.v[C::SHP + tid];
+  if (UNI && tid < 64) {
+    const int ca = tid >> 3, k = tid & 7;
+    const int comp = k < 6 ? (k >> 1) : (k - 6);  // x x y y z z x y
+    cw2[ca][k] = -(a.rp.v[C::DET] * a.rp.v[C::SHP + 3 * ca + comp]);
+  }
   __syncthreads();
   int nb;
   const int M = stage_nodes(g, tile, a.vel32, a.dl32, a.nnode, Mmax, ts, nb);
@@ -231,12 +237,15 @@ __device__ __forceinline__ void pml_rec_body(const ElemArgs32 &a, int tile) {
   }
   __syncthreads();
   if (UNI) {
-    auto w_of = [&](int, int c, float &wx, float &wy, float &wz) {
-      wx = cw[3 * c];
-      wy = cw[3 * c + 1];
-      wz = cw[3 * c + 2];
+    auto w2_of = [&](int, int c, float2 &wxx, float2 &wyy, float2 &wzz, float2 &wxy) {
+      const float4 p = *reinterpret_cast<const float4 *>(&cw2[c][0]);
+      const float4 q = *reinterpret_cast<const float4 *>(&cw2[c][4]);
+      wxx = make_float2(p.x, p.y);
+      wyy = make_float2(p.z, p.w);
+      wzz = make_float2(q.x, q.y);
+      wxy = make_float2(q.z, q.w);
     };
-    pml_gather(g, M, nb, incp, sinc, es, cfh, w_of, a.F, a.F9, a.nnode, a.n_int, a.npml, ts.sids);
+    pml_gather(g, M, nb, incp, sinc, es, cfh, w2_of, a.F, a.F9, a.nnode, a.n_int, a.npml, ts.sids);
   } else {
     auto src_of = [&](int el) {
       return RecSrc<L>{rec + (size_t)row_u32(tab, L::RID, el) * rlen, tab, el, nullptr, 0, 0u, 0u};

@@ -31,6 +31,13 @@ typedef struct eqd_case eqd_case;
  * writes a message retrievable with eqd_case_last_error(). */
 int eqd_case_build(const char *dir, eqd_case **out);
 
+/* eqd_case_build with options: flags = EQD_CASE_MESH_ONLY builds the mesh, materials, fault and
+ * stations but not the per-element tables or nodal masses (eleshp, eledet, elemass, ss, phi,
+ * nodalMassArr and fnms are NULL in the view; about 700 bytes per element less host memory), for
+ * eqd_gpu_init to build them on the device. */
+#define EQD_CASE_MESH_ONLY 1
+int eqd_case_build_opt(const char *dir, int32_t flags, eqd_case **out);
+
 /* Views into the case's arrays (owned by the case; valid until eqd_case_free). */
 int eqd_case_view(eqd_case *c, eqd_scalars *s, eqd_host_arrays *a);
 

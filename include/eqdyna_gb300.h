@@ -333,6 +333,21 @@ int eqd_gpu_table_info(eqd_context *ctx, int32_t group, int64_t info[8]);
 int eqd_host_element_order(const eqd_host_arrays *a, int32_t group, int32_t tile_shape, int32_t *out,
                            int64_t cap, int64_t *n_out, double *live);
 
+/* Setup on the GPU: the per-element tables and lumped nodal masses that the reference builds on
+ * the host before its time loop (assembleGlobalMass, src/assembleGlobalMass.f90:12-38,283-406;
+ * calcGlobalShapeFunc, src/calcGlobalShapeFunc.f90:1-75; calcSSPhi4Hrgls,
+ * src/assembleGlobalMass.f90:328-374), computed on `device` from the mesh arrays of `a` (nnode,
+ * nelem, nodeElemIdRelation, elemTypeArr, meshCoor, mat; for nodalMassArr also neq,
+ * eqNumIndexArr, eqNumStartIndexLoc, numOfDofPerNodeArr) and written in the Fortran layout to the
+ * output arrays that are not NULL: eleshp (3, 8, nelem), eledet (nelem), elemass (24, nelem),
+ * ss (6, nelem), phi (8, 4, nelem), nodalMassArr (neq), fnms (nnode).  The values are bit for bit
+ * those of the reference's host arithmetic (no contraction; a node's mass is summed element by
+ * element in the reference's order).  EQD_ERR_INPUT for a node id out of range or a non-positive
+ * determinant.  eqd_gpu_init computes the same tables on the device when the caller passes NULL
+ * for all of eleshp, eledet, elemass, ss, phi, nodalMassArr and fnms. */
+int eqd_gpu_element_tables(int32_t device, const eqd_host_arrays *a, double *eleshp, double *eledet,
+                           double *elemass, double *ss, double *phi, double *nodalMassArr, double *fnms);
+
 /* Measured binary64 fused-multiply-add throughput of a device (TFLOP/s, 2 flops per FMA),
  * from a register-resident FMA chain kernel; used as the compute roofline of the FP64 form. */
 int eqd_gpu_fp64_fma_peak(int32_t device, double *tflops);

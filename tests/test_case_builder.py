@@ -137,3 +137,26 @@ def test_arrays_outlive_the_case_and_clones_are_private():
     del case, twin
     gc.collect()
     assert float(coor.sum()) == expect
+
+
+TABLES = ("eleshp", "eledet", "elemass", "ss", "phi", "nodalMassArr", "fnms")
+
+
+def test_mesh_only_build_has_everything_but_the_tables():
+    """Case.from_dir(tables=False) (eqd_case_build_opt with EQD_CASE_MESH_ONLY) leaves the seven
+    table arrays out, for eqd_gpu_init to build them on the device, and gives every other array
+    byte for byte as the full build does (a C3 mesh: wedges, a dipping fault, a stretched PML)."""
+    import tempfile
+    from eqdyna_gb300.case import Case
+    from eqdyna_gb300.configs import config_c3
+    d = config_c3(tempfile.mkdtemp(prefix="eqd_c3m_"), scale=4.0, nsteps=10)
+    full, mesh = Case.from_dir(d), Case.from_dir(d, tables=False)
+    for k, v in full.arrays.items():
+        if k in TABLES:
+            assert v is not None and mesh.arrays[k] is None, k
+        elif v is None:
+            assert mesh.arrays[k] is None, k
+        else:
+            assert np.array_equal(v, mesh.arrays[k]), k
+    assert full.sizes == mesh.sizes
+    assert bytes(full.scalars) == bytes(mesh.scalars)
