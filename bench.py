@@ -146,11 +146,15 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def build_case(config, scale, nsteps, workdir):
+def build_case(config, scale, nsteps, workdir, tables=True, hourglass=0):
+    """The configuration's case; tables=False builds the mesh only (eqd_gpu_init then builds the
+    per-element tables and nodal masses on the device); hourglass = 1 or 2 sets C_hg (C0 only:
+    its "hourglass coefficient 0.1" is the viscous form's kapa_hg)."""
     from eqdyna_gb300 import configs
     from eqdyna_gb300.case import Case
-    configs.CONFIGS[config](workdir, scale=scale, nsteps=nsteps)
-    return Case.from_dir(workdir)
+    extra = {"C_hg": hourglass} if (hourglass and config == "C0") else {}
+    configs.CONFIGS[config](workdir, scale=scale, nsteps=nsteps, **extra)
+    return Case.from_dir(workdir, tables=tables)
 
 
 def algorithmic_bytes(case, precision, tables=None):
@@ -386,7 +390,8 @@ def bench_ours(args, world, rank, local):
     tmp = tempfile.mkdtemp(prefix="eqd_bench_")
     job = args.job_steps if args.job_steps > 0 else JOB_STEPS[args.config]
     total_steps = max(job, args.warmup + min(args.steps, 40) + args.steps + 4)
-    case = build_case(args.config, args.scale, total_steps, tmp)
+    mesh_only = bool(args.mesh_only) if args.mesh_only >= 0 else (args.config == "C2" and args.scale < 1.5)
+    case = build_case(args.config, args.scale, total_steps, tmp, tables=not mesh_only, hourglass=args.hourglass)
     shutil.rmtree(tmp, ignore_errors=True)
     ne = case.sizes["nelem"]
     host_bytes_in = sum(v.nbytes for k, v in case.arrays.items() if v is not None)
@@ -585,7 +590,9 @@ def bench_ours(args, world, rank, local):
         roofline["frac_dram"] = d["frac_dram"]
     if args.precision == "fp64":
         roofline["fp64"] = fp64_compute_roofline(kt, ab, lib, local)
-    cpu = run_cpu_baseline(case, args.cpu_seconds) if (rank == 0 and world == 1 and args.cpu_seconds > 0) else None
+    # (the oracle reads the host tables, which a mesh-only case does not have)
+    cpu = (run_cpu_baseline(case, args.cpu_seconds)
+           if (rank == 0 and world == 1 and args.cpu_seconds > 0 and not mesh_only) else None)
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": dev_s * 1e3 / args.steps, "higher_is_better": True,
@@ -594,6 +601,8 @@ def bench_ours(args, world, rank, local):
             "data": "synthetic (seeded config generator, no external dataset)",
             "config": {"workload": f"{args.config}: {WORKLOADS[args.config]}", "elements": ne,
                        "physical_elements": case.dims["n_phys_elem"], "precision": args.precision,
+                       "hourglass": {1: "stiffness (KF78)", 2: f"viscous, kapa_hg {case.scalars.kapa_hg}"}[
+                           case.scalars.C_hg],
                        "learned_guess": bool(args.learned), "scale": args.scale,
                        "l2": f"inputs larger than L2: working set {working_set / 1e9:.2f} GB per step "
                              "vs 129 MB L2, no flush",
@@ -603,6 +612,7 @@ def bench_ours(args, world, rank, local):
                                               "live_slots": round(v["elements"] / max(v["slots"], 1), 4)}
                                           for k, v in tables.items()},
                        "launch": launch or "defaults",
+                       "setup_tables": "device (mesh-only host case)" if mesh_only else "host case builder",
                        "parallelism": "replicas" if world > 1 else "single GPU",
                        "setup_s": round(setup_s, 1), "setup_phases_s": case.build_phases_s,
                        "wall_ms_per_step": wall * 1e3 / args.steps,
@@ -735,6 +745,11 @@ def main():
     ap.add_argument("--plain-check", type=int, default=1,
                     help="also run the plain binary64 method on the same steps (speed and accuracy)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--hourglass", type=int, default=0, choices=[0, 1, 2],
+                    help="C0: hourglass form, 1 stiffness (KF78), 2 viscous with kapa_hg 0.1 (0: the config's)")
+    ap.add_argument("--mesh-only", type=int, default=-1,
+                    help="1: host case without element tables, built on the device by eqd_gpu_init; 0: host "
+                         "tables; -1: by size (C2 at its stated size)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -29,7 +29,7 @@ __global__ void __launch_bounds__(kBlockElem)
                       ElemConst k) {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= g.ne) return;
-  const int ne = g.ne;
+  const size_t ne = g.ne;  // 64-bit: the 32 hourglass rows of a group of 10^8 elements pass 2^31
   int n[8];
 #pragma unroll
   for (int a = 0; a < 8; ++a) n[a] = __ldg(g.conn + a * ne + e);
@@ -209,7 +209,7 @@ __global__ void __launch_bounds__(kBlockElem)
                  int nnode, int n_int, int npml, ElemConst k) {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= g.ne) return;
-  const int ne = g.ne;
+  const size_t ne = g.ne;  // 64-bit: the 32 hourglass rows of a group of 10^8 elements pass 2^31
   int n[8];
 #pragma unroll
   for (int a = 0; a < 8; ++a) n[a] = __ldg(g.conn + a * ne + e);
