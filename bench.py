@@ -576,7 +576,9 @@ def bench_ours(args, world, rank, local):
     # ---- rooflines: every kernel, the one with the largest time share on top ----
     ab = algorithmic_bytes(case, args.precision, tables)
     working_set = ab["interior"][0] + ab["pml"][0] + ab["node"][0]
-    per_kernel = kernel_rooflines(kt, ab, args.precision, tables, hbm_peak, NCU_TRAFFIC_PER_UNIT)
+    # the measured traffic per unit belongs to the mesh it was captured on: full-size C1
+    measured = NCU_TRAFFIC_PER_UNIT if (args.config == "C1" and args.scale == 1.0) else None
+    per_kernel = kernel_rooflines(kt, ab, args.precision, tables, hbm_peak, measured)
     step_ms_total = kt["step"][0]
     dom = max(per_kernel, key=lambda k: per_kernel[k]["share"])
     d = per_kernel[dom]
@@ -673,7 +675,7 @@ def bench_ensemble(args, world, rank, local):
     barrier(world)
     t0 = time.perf_counter()
     solvers = [GpuSolver(c.clone(), precision="fp32", device=local) for c in cases]
-    ens = Ensemble(solvers)
+    ens = Ensemble(solvers, persistent=args.ens_mode == 1)
     t_init = time.perf_counter() - t0
     for _ in range(job):
         ens.step(1)
@@ -691,7 +693,7 @@ def bench_ensemble(args, world, rank, local):
 
     # ---- device-timed steps ----
     solvers = [GpuSolver(c.clone(), precision="fp32", device=local) for c in cases]
-    ens = Ensemble(solvers)
+    ens = Ensemble(solvers, persistent=args.ens_mode == 1)
     ens.step(args.warmup)
     barrier(world)
     with ClockSampler(local) as clk:
@@ -711,6 +713,8 @@ def bench_ensemble(args, world, rank, local):
             "config": {"workload": f"C4: {WORKLOADS['C4']}", "members": args.members, "elements": int(total),
                        "member_elements": [min(ne), max(ne)], "members_per_dx": dxs,
                        "precision": "fp32", "parallelism": "replicas" if world > 1 else "single GPU",
+                       "launch": "one persistent cooperative launch per call" if args.ens_mode == 1
+                                 else "one launch per kernel per step, 16-step graphs",
                        "l2": "inputs larger than L2, no flush", "setup_s": round(setup_s, 1)},
             "e2e": {"value": total * job * world / e2e_s, "unit": UNIT, "steps": job,
                     "init_s": round(t_init, 2),
@@ -720,7 +724,7 @@ def bench_ensemble(args, world, rank, local):
                     "note": "whole ensemble job through the C ABI: init of every member, one ensemble step "
                             "per call followed by a read of every member's peak slip rate into pinned "
                             "memory, final fetch of every member"},
-            "gpu_launches": 4 * args.steps, "clocks": clk.summary()}
+            "gpu_launches": 1 if args.ens_mode == 1 else 4 * args.steps, "clocks": clk.summary()}
     return line if rank == 0 else None
 
 
@@ -739,6 +743,8 @@ def main():
     ap.add_argument("--job-steps", type=int, default=0, help="steps of the end-to-end job (0: the config's)")
     ap.add_argument("--tuned", type=int, default=1, help="use the autotuned launch shapes when recorded")
     ap.add_argument("--members", type=int, default=64, help="C4 ensemble size")
+    ap.add_argument("--ens-mode", type=int, default=0, choices=[0, 1],
+                    help="C4: 0 batched launches in step graphs, 1 one persistent launch per call")
     ap.add_argument("--tables", default="auto", choices=["auto", "streamed", "records"],
                     help="binary32 element-table layout")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])

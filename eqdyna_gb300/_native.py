@@ -207,7 +207,9 @@ def gpu_lib():
         lib.eqd_ensemble_step.argtypes = [C.c_void_p, C.c_int32]
         lib.eqd_ensemble_destroy.argtypes = [C.c_void_p]
         lib.eqd_ensemble_time.argtypes = [C.c_void_p, d_p]
-        for name in ("eqd_ensemble_create", "eqd_ensemble_step", "eqd_ensemble_destroy", "eqd_ensemble_time"):
+        lib.eqd_ensemble_mode.argtypes = [C.c_void_p, C.c_int32]
+        for name in ("eqd_ensemble_create", "eqd_ensemble_step", "eqd_ensemble_destroy", "eqd_ensemble_time",
+                     "eqd_ensemble_mode"):
             getattr(lib, name).restype = C.c_int
         lib.eqd_gpu_newton_counts.argtypes = [C.c_void_p, C.POINTER(C.c_int64)]
         lib.eqd_gpu_newton_counts.restype = C.c_int
@@ -231,6 +233,7 @@ GPU_SYMBOLS = ["eqd_gpu_init", "eqd_gpu_step", "eqd_gpu_fetch", "eqd_gpu_fetch_f
                "eqd_gpu_fetch_fric_rows_async", "eqd_gpu_fetch_wait", "eqd_gpu_output_setup",
                "eqd_gpu_output_drain",
                "eqd_ensemble_create", "eqd_ensemble_step", "eqd_ensemble_destroy", "eqd_ensemble_time",
+               "eqd_ensemble_mode",
                "eqd_gpu_init_times",
                "eqd_gpu_newton_log", "eqd_gpu_newton_records", "eqd_gpu_mlp_train", "eqd_gpu_mlp_get",
                "eqd_gpu_mlp_set", "eqd_gpu_mlp_enable", "eqd_gpu_newton_replay", "eqd_mlp_gradient",

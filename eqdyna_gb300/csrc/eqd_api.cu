@@ -1921,6 +1921,8 @@ struct eqd_ensemble {
   cudaGraphExec_t graph = nullptr;
   cudaEvent_t ev[2] = {nullptr, nullptr};
   double last_ms = 0.0;
+  int mode = 0;              // 0 batched launches in step graphs, 1 one persistent launch per call
+  unsigned *bar = nullptr;   // grid-barrier words of the persistent launch
 };
 
 namespace {
@@ -1991,6 +1993,10 @@ int eqd_ensemble_step(eqd_ensemble *E, int32_t nsteps) {
     EQD_CUDA_OK(cudaEventRecord(E->ev[0], E->stream));
     ++done;
   }
+  if (E->mode == 1 && nsteps > done) {  // every remaining step in one cooperative launch
+    RC(launch_ensemble_persistent(E->nf, E->eb, nsteps - done, E->bar, E->ctx[0]->d_err, E->stream));
+    done = nsteps;
+  }
   if (nsteps - done >= kGraphSteps) {
     if (!E->graph) {
       cudaGraph_t g;
@@ -2044,8 +2050,30 @@ int eqd_ensemble_destroy(eqd_ensemble *E) {
     if (e) cudaEventDestroy(e);
   node_fault_batch_free(E->nf);
   elem_batch_free(E->eb);
+  if (E->bar) cudaFree(E->bar);
   if (E->stream) cudaStreamDestroy(E->stream);
   delete E;
+  return EQD_OK;
+}
+
+int eqd_ensemble_mode(eqd_ensemble *E, int32_t mode) {
+  if (!E) return EQD_ERR_STATE;
+  if (mode != 0 && mode != 1) return EQD_ERR_INPUT;
+  if (mode == 1) {
+    for (auto *c : E->ctx)
+      if (c->sc.friclaw > 2 || c->sc.C_Q != 0 || ((c->sc.rdampm != 0.0) && c->sc.C_elastic != 0))
+        return EQD_ERR_UNSUPPORTED;
+    cudaSetDevice(E->device);
+    if (!E->bar && cudaMalloc(&E->bar, 2 * sizeof(unsigned)) != cudaSuccess) {
+      cudaGetLastError();
+      E->bar = nullptr;
+      return EQD_ERR_OOM;
+    }
+    int coop = 0;
+    EQD_CUDA_OK(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, E->device));
+    if (!coop) return EQD_ERR_UNSUPPORTED;
+  }
+  E->mode = mode;
   return EQD_OK;
 }
 

@@ -192,6 +192,16 @@ void node_fault_batch_free(void *handle);
 int elem_batch_update(void **handle, Context *const *members, int n, const ElemConst *k);
 int launch_elements_batched(const void *handle, cudaStream_t s, int part);
 void elem_batch_free(void *handle);
+// The element tables of an ensemble for the persistent kernel: device argument arrays
+// (ElemArgs32 of elem32r_body.cuh) and tile prefix sums of both groups, tiles and largest tile node
+// count per group, and the kernel variant {body, plastic, s0, hg, q}.
+int elem_batch_tables(const void *handle, const void *args[2], const int *start[2], int tiles[2], int Mmax[2],
+                      int variant[5]);
+// Advances every member of an ensemble by nsteps steps (none the first of its run) in one
+// cooperative launch; bar: 2 device words, zero between launches; EQD_ERR_UNSUPPORTED when a member
+// runs rate-and-state friction or the binary32 Q form (the batched launches cover those).
+int launch_ensemble_persistent(const void *nf, const void *eb, int nsteps, unsigned *bar, int *err,
+                               cudaStream_t s);
 int mlp_init(Context &c);
 void mlp_free(Context &c);
 int newton_log_start(Context &c, int nsteps, int stride);

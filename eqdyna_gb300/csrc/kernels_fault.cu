@@ -7,12 +7,14 @@
 // fault_kernel : one thread per split-node pair: thermop (src/thermop.f90), faulting
 //                (src/faulting.f90:3-541) with the friction laws (src/fric.f90), station capture
 //                (src/faulting.f90:518-541, src/driver.f90:157-180) and rupture time.
+#include <algorithm>
 #include <vector>
 
 #include "eqd_device.cuh"
 #include "fpconv.cuh"
 #include "mlp_common.cuh"
 #include "rsf_newton.cuh"
+#include "elem32r_body.cuh"
 
 namespace eqd {
 
@@ -349,7 +351,9 @@ __global__ void __launch_bounds__(32 * kTpWarps) thermop_kernel(FaultArgs p) {
   }
 }
 
-template <bool F32>
+// RSF = false leaves the rate-and-state branch (friclaw 3-5) out of the instantiation: a kernel
+// that runs slip- or time-weakening faults only then carries none of the Newton solve's registers.
+template <bool F32, bool RSF = true>
 __device__ __forceinline__ void fault_body(const FaultArgs &p, int tid,
                                            __nv_bfloat16 (*mlp_xs)[32 * kMlpK1]) {
   const int nt = *p.d_nt;
@@ -427,7 +431,7 @@ __device__ __forceinline__ void fault_body(const FaultArgs &p, int tid,
           init[1] * p.C_elastic;
   tr[2] = (mSM * (q[2][1][1] - q[2][0][1]) / dt + mS * q[2][1][0] - mM * q[2][0][0]) / totalMass +
           init[2] * p.C_elastic;
-  if (p.friclaw >= 3 && p.C_nuclea_here) {  // rsfNucleation (src/faulting.f90:367-414)
+  if (RSF && p.friclaw >= 3 && p.C_nuclea_here) {  // rsfNucleation (src/faulting.f90:367-414)
     double dtau = 0.0, Fn = 0.0, G = 1.0;
     if (radius < p.nucR) Fn = exp(radius * radius / (radius * radius - p.nucR * p.nucR));
     if (t <= p.nucT) G = exp((t - p.nucT) * (t - p.nucT) / (t * (t - 2.0 * p.nucT)));
@@ -448,7 +452,7 @@ __device__ __forceinline__ void fault_body(const FaultArgs &p, int tid,
   tr[3] = sqrt(tr[1] * tr[1] + tr[2] * tr[2]);
 
   unsigned iters = 0, maxhit = 0, executed = 0, learned = 0, fallback = 0;
-  if (p.friclaw <= 2) {
+  if (!RSF || p.friclaw <= 2) {
     // solveSWTW (src/faulting.f90:136-188)
     double mu;
     if (p.friclaw == 1) {
@@ -491,7 +495,7 @@ __device__ __forceinline__ void fault_body(const FaultArgs &p, int tid,
     FR(78) = tr[0];
     FR(79) = tr[1];
     FR(80) = tr[2];
-  } else {
+  } else if constexpr (RSF) {
     // solveRSF (src/faulting.f90:190-327)
     tr[0] += (p.friclaw == 5) ? FR(51) : FR(6);
     if (p.insertFaultType > 0 && p.C_elastic == 1) {
@@ -588,7 +592,7 @@ __device__ __forceinline__ void fault_body(const FaultArgs &p, int tid,
       FR(34 + j) = p.vel[j * nn + sl] + (-xa + R / mM) * dt;
     }
   }
-  if (p.friclaw >= 3) {
+  if (RSF && p.friclaw >= 3) {
     warp_count_add(p.stats + 0, iters);
     warp_count_add(p.stats + 1, maxhit);
     warp_count_add(p.stats + 2, executed);
@@ -748,6 +752,9 @@ struct NodeFaultBatch {
   FaultArgs *d_fault = nullptr;
   int *d_node_start = nullptr, *d_fault_start = nullptr;  // [n + 1] block prefix sums
   int node_blocks = 0, fault_blocks = 0;
+  int *d_node_start_tile = nullptr;  // [n + 1] prefix sums of blocks of kTile nodes (persistent kernel)
+  int node_blocks_tile = 0;
+  int max_friclaw = 0;
   std::vector<NodeArgs32> h_node;
   std::vector<FaultArgs> h_fault;
 };
@@ -769,6 +776,17 @@ int node_fault_batch_update(void **handle, Context *const *m, int n) {
     }
     b->node_blocks = ns[n];
     b->fault_blocks = fs[n];
+    std::vector<int> nt(n + 1, 0);
+    for (int i = 0; i < n; ++i) {
+      nt[i + 1] = nt[i] + (m[i]->nnode + kTile - 1) / kTile;
+      b->max_friclaw = std::max(b->max_friclaw, m[i]->sc.friclaw);
+    }
+    b->node_blocks_tile = nt[n];
+    if (cudaMalloc(&b->d_node_start_tile, sizeof(int) * (n + 1)) != cudaSuccess) {
+      node_fault_batch_free(b);
+      return EQD_ERR_OOM;
+    }
+    cudaMemcpy(b->d_node_start_tile, nt.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice);
     if (cudaMalloc(&b->d_node, sizeof(NodeArgs32) * n) != cudaSuccess ||
         cudaMalloc(&b->d_fault, sizeof(FaultArgs) * n) != cudaSuccess ||
         cudaMalloc(&b->d_node_start, sizeof(int) * (n + 1)) != cudaSuccess ||
@@ -811,7 +829,187 @@ void node_fault_batch_free(void *handle) {
   if (b->d_fault) cudaFree(b->d_fault);
   if (b->d_node_start) cudaFree(b->d_node_start);
   if (b->d_fault_start) cudaFree(b->d_fault_start);
+  if (b->d_node_start_tile) cudaFree(b->d_node_start_tile);
   delete b;
+}
+
+// ---- persistent ensemble step ------------------------------------------------------------------
+// One cooperative launch advances every member by many steps: per step the node update of every
+// member, then the interior and PML tiles of every member, then the fault pairs (and station rows)
+// of every member, each phase split over the resident CTAs and closed by a grid-wide barrier.  The
+// device bodies are those of the batched launches, so the arithmetic is the same.
+namespace {
+
+static_assert(kBlockFault == kTile, "fault blocks and tiles share the persistent CTA");
+constexpr unsigned long long kGridWaitNs = 2000000000ull;  // a barrier wait gives up after 2 s
+constexpr unsigned kGridWaitPolls = 1u << 26;             // or after this many polls
+
+struct PersistentArgs {
+  const NodeArgs32 *node;
+  const int *node_start;      // [n + 1] prefix sums of blocks of kTile nodes
+  int node_blocks;
+  const ElemArgs32 *elem[2];  // interior, PML
+  const int *elem_start[2];   // [n + 1] tile prefix sums
+  int tiles[2];
+  const FaultArgs *fault;
+  const int *fault_start;     // [n + 1] prefix sums of blocks of kBlockFault pairs
+  int fault_blocks;
+  int n, nsteps;
+  unsigned *bar;  // [0] arrivals, [1] generation; zero at launch
+  int *err;       // bit 2 set when a barrier wait gave up
+};
+
+// Grid-wide barrier of a cooperative launch (all CTAs resident).  Thread 0 of each CTA arrives on
+// the counter; the last one resets it and advances the generation the others wait for.  The wait is
+// bounded in polls and in time: a CTA that gives up flags bit 2 of the error word and returns false,
+// and every other CTA then gives up at a barrier too.
+__device__ __forceinline__ bool grid_barrier(unsigned *bar, int *err) {
+  __shared__ int ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    ok = 1;
+    volatile unsigned *gen = bar + 1;
+    const unsigned g = *gen;
+    __threadfence();
+    if (atomicAdd(bar, 1u) == gridDim.x - 1) {
+      atomicExch(bar, 0u);
+      __threadfence();
+      atomicAdd(bar + 1, 1u);
+    } else {
+      const unsigned long long t0 = globaltimer_ns();
+      for (unsigned it = 0; *gen == g; ++it) {
+        if (it >= kGridWaitPolls || ((it & 255u) == 255u && globaltimer_ns() - t0 > kGridWaitNs)) {
+          atomicOr(err, 2);
+          ok = 0;
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
+template <class T>
+__device__ __forceinline__ void copy_args(T *dst, const T *src) {
+  static_assert(sizeof(T) % 4 == 0, "argument block of whole words");
+  const int *s = reinterpret_cast<const int *>(src);
+  int *d = reinterpret_cast<int *>(dst);
+  for (int q = threadIdx.x; q < (int)(sizeof(T) / 4); q += blockDim.x) d[q] = s[q];
+}
+
+// Slip- and time-weakening members only (the fault body without the Newton solve), no Q; every
+// step but a member's first (stored acceleration).  At most 72 registers a thread: 7 CTAs of
+// kTile threads per SM, as many as the element passes' shared memory allows.
+template <bool BODY, bool PLASTIC, int HG, bool S0>
+__global__ void __launch_bounds__(kTile, 7) ensemble_persistent(const __grid_constant__ PersistentArgs P) {
+  __shared__ __align__(16) NodeArgs32 na;
+  __shared__ __align__(16) ElemArgs32 ea;
+  __shared__ __align__(16) FaultArgs fa;
+  __shared__ int lb;
+  for (int step = 0; step < P.nsteps; ++step) {
+    for (int b = blockIdx.x; b < P.node_blocks; b += gridDim.x) {
+      const int m = batch_member(P.node_start, P.n, b);
+      copy_args(&na, P.node + m);
+      if (threadIdx.x == 0) lb = b - P.node_start[m];
+      __syncthreads();
+      const int i = lb * kTile + threadIdx.x;
+      if (na.damp) node_update32_body<false, true>(na, i);
+      else node_update32_body<false, false>(na, i);
+      __syncthreads();
+    }
+    if (!grid_barrier(P.bar, P.err)) return;
+    for (int grp = 0; grp < 2; ++grp) {
+      for (int b = blockIdx.x; b < P.tiles[grp]; b += gridDim.x) {
+        const int m = elem_batch_member(P.elem_start[grp], P.n, b);
+        copy_args(&ea, P.elem[grp] + m);
+        __syncthreads();
+        const int tile = b - P.elem_start[grp][m];
+        if (grp == 0) {
+          if (ea.g.nrec == 1) interior_rec_body<BODY, PLASTIC, HG, true, false>(ea, tile);
+          else interior_rec_body<BODY, PLASTIC, HG, false, false>(ea, tile);
+        } else {
+          if (ea.g.nrec == 1) pml_rec_body<BODY, S0, HG, true>(ea, tile);
+          else pml_rec_body<BODY, S0, HG, false>(ea, tile);
+        }
+        __syncthreads();  // the next tile's copies land in the same shared memory
+      }
+    }
+    if (!grid_barrier(P.bar, P.err)) return;
+    for (int b = blockIdx.x; b < P.fault_blocks; b += gridDim.x) {
+      const int m = batch_member(P.fault_start, P.n, b);
+      copy_args(&fa, P.fault + m);
+      if (threadIdx.x == 0) lb = b - P.fault_start[m];
+      __syncthreads();
+      fault_body<true, false>(fa, lb * kTile + threadIdx.x, nullptr);
+      __syncthreads();
+    }
+    if (!grid_barrier(P.bar, P.err)) return;
+  }
+}
+
+template <bool BODY, bool PLASTIC, int HG, bool S0>
+int launch_persistent_variant(const PersistentArgs &P, const int Mmax[2], cudaStream_t s) {
+  auto kern = ensemble_persistent<BODY, PLASTIC, HG, S0>;
+  const size_t sm = std::max(rec_smem<RecInterior<BODY, PLASTIC, HG, false>>(std::max(Mmax[0], 1)),
+                             rec_smem<RecPml<BODY, S0, HG>>(std::max(Mmax[1], 1)));
+  if (allow_smem(kern, sm)) return EQD_ERR_CUDA;
+  int dev = 0, nsm = 0, per = 0;
+  EQD_CUDA_OK(cudaGetDevice(&dev));
+  EQD_CUDA_OK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  EQD_CUDA_OK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, kTile, sm));
+  if (per <= 0) return EQD_ERR_UNSUPPORTED;
+  const int work = std::max({P.node_blocks, P.tiles[0], P.tiles[1], P.fault_blocks, 1});
+  const int grid = std::min(per * nsm, work);
+  void *args[] = {const_cast<PersistentArgs *>(&P)};
+  EQD_CUDA_OK(cudaLaunchCooperativeKernel(reinterpret_cast<const void *>(kern), dim3(grid), dim3(kTile), args, sm, s));
+  return EQD_OK;
+}
+
+}  // namespace
+
+int launch_ensemble_persistent(const void *nf, const void *eb, int nsteps, unsigned *bar, int *err,
+                               cudaStream_t s) {
+  const NodeFaultBatch *b = static_cast<const NodeFaultBatch *>(nf);
+  if (!b || !eb || nsteps <= 0) return EQD_ERR_STATE;
+  if (b->max_friclaw > 2) return EQD_ERR_UNSUPPORTED;
+  PersistentArgs P{};
+  const void *eargs[2];
+  const int *estart[2];
+  int tiles[2], Mmax[2], v[5];
+  const int rc = elem_batch_tables(eb, eargs, estart, tiles, Mmax, v);
+  if (rc) return rc;
+  const bool body = v[0], plastic = v[1], s0 = v[2];
+  const int hg = v[3];
+  if (v[4] || (body != plastic)) return EQD_ERR_UNSUPPORTED;  // Q, or mass damping without plasticity
+  P.node = b->d_node;
+  P.node_start = b->d_node_start_tile;
+  P.node_blocks = b->node_blocks_tile;
+  for (int grp = 0; grp < 2; ++grp) {
+    P.elem[grp] = static_cast<const ElemArgs32 *>(eargs[grp]);
+    P.elem_start[grp] = estart[grp];
+    P.tiles[grp] = tiles[grp];
+  }
+  P.fault = b->d_fault;
+  P.fault_start = b->d_fault_start;
+  P.fault_blocks = b->fault_blocks;
+  P.n = b->n;
+  P.nsteps = nsteps;
+  P.bar = bar;
+  P.err = err;
+  EQD_CUDA_OK(cudaMemsetAsync(bar, 0, 2 * sizeof(unsigned), s));
+  if (hg == 2) {
+    if (plastic) return s0 ? launch_persistent_variant<true, true, 2, true>(P, Mmax, s)
+                           : launch_persistent_variant<true, true, 2, false>(P, Mmax, s);
+    return s0 ? launch_persistent_variant<false, false, 2, true>(P, Mmax, s)
+              : launch_persistent_variant<false, false, 2, false>(P, Mmax, s);
+  }
+  if (plastic) return s0 ? launch_persistent_variant<true, true, 1, true>(P, Mmax, s)
+                         : launch_persistent_variant<true, true, 1, false>(P, Mmax, s);
+  return s0 ? launch_persistent_variant<false, false, 1, true>(P, Mmax, s)
+            : launch_persistent_variant<false, false, 1, false>(P, Mmax, s);
 }
 
 namespace {

@@ -108,6 +108,14 @@ module eqd_gpu_mod
       import :: c_int, c_ptr
       type(c_ptr), value :: p
     end function
+    ! setup on the GPU: the tables of assembleGlobalMass from the mesh (any output may be c_null_ptr)
+    integer(c_int) function eqd_gpu_element_tables(device, a, eleshp, eledet, elemass, ss, phi, &
+        nodalMassArr, fnms) bind(C, name="eqd_gpu_element_tables")
+      import :: c_int, c_int32_t, c_ptr, eqd_host_arrays
+      integer(c_int32_t), value :: device
+      type(eqd_host_arrays), intent(in) :: a
+      type(c_ptr), value :: eleshp, eledet, elemass, ss, phi, nodalMassArr, fnms
+    end function
     integer(c_int) function eqd_gpu_elem_forces_noalloc(view, force_out, stream) &
         bind(C, name="eqd_gpu_elem_forces_noalloc")
       import :: c_int, c_ptr, eqd_elem_device_view

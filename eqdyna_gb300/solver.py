@@ -271,7 +271,7 @@ class Ensemble:
     """Several GpuSolver members (scenarios of any size and time step, binary32 form with
     record-indexed tables) advanced together: one launch per kernel per step over all members."""
 
-    def __init__(self, solvers):
+    def __init__(self, solvers, persistent=False):
         self.lib = N.gpu_lib()
         self.solvers = list(solvers)
         hs = (C.c_void_p * len(self.solvers))(*[s._h for s in self.solvers])
@@ -280,6 +280,14 @@ class Ensemble:
         if rc != 0:
             raise N.EqdError(rc, "eqd_ensemble_create")
         self._h = h
+        if persistent:
+            self.set_mode(1)
+
+    def set_mode(self, mode):
+        """0: one launch per kernel per step, step graphs; 1: one persistent launch per step() call."""
+        rc = self.lib.eqd_ensemble_mode(self._h, int(mode))
+        if rc != 0:
+            raise N.EqdError(rc, "eqd_ensemble_mode")
 
     def step(self, nsteps=1):
         rc = self.lib.eqd_ensemble_step(self._h, int(nsteps))

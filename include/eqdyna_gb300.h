@@ -310,6 +310,14 @@ int eqd_ensemble_create(eqd_context *const *members, int32_t n, eqd_ensemble **e
 /* Advances every member by nsteps steps (each from its own current step). */
 int eqd_ensemble_step(eqd_ensemble *ens, int32_t nsteps);
 int eqd_ensemble_destroy(eqd_ensemble *ens);
+/* How eqd_ensemble_step runs the steps: mode 0 (default) one launch per kernel per step over all
+ * members, 16 steps captured in a CUDA graph; mode 1 every step of a call (after a member's first)
+ * in ONE persistent cooperative launch: the node update, interior and PML element tiles and fault
+ * pairs of all members, each phase split over the resident CTAs and closed by a grid barrier whose
+ * waits are bounded (a wait that gives up returns EQD_ERR_TIMEOUT from the step).  Mode 1 serves
+ * slip- and time-weakening members without Q (EQD_ERR_UNSUPPORTED otherwise); results agree with
+ * mode 0 to the round-off of the binary32 reductions. */
+int eqd_ensemble_mode(eqd_ensemble *ens, int32_t mode);
 /* Device time (ms, CUDA events on the ensemble's stream) of the last eqd_ensemble_step call. */
 int eqd_ensemble_time(eqd_ensemble *ens, double *ms);
 

@@ -88,3 +88,59 @@ def test_ensemble_rejects_streamed_members():
     finally:
         for s in solvers:
             s.close()
+
+
+def test_persistent_launch_matches_batched_launches():
+    """eqd_ensemble_mode 1: every step of a call in one persistent cooperative launch (node update,
+    element tiles and fault pairs of all members, phases closed by bounded grid barriers).  Each
+    member agrees with the batched launches (mode 0) to relative 1e-4 and stays within the binary32
+    budget against the oracle; both device times are printed."""
+    from conftest import nthreads
+    from eqdyna_gb300.solver import Ensemble, GpuSolver
+    from oracle import Oracle
+    from test_gpu_fp32 import _check, _errors
+    cases = _cases()
+    runs, times = {}, {}
+    for mode in (0, 1):
+        members = [c.clone() for c in cases]
+        solvers = [GpuSolver(g, precision="fp32", table_layout="records") for g in members]
+        try:
+            with Ensemble(solvers, persistent=(mode == 1)) as e:
+                e.step(1)
+                e.step(NSTEPS - 1)
+                times[mode] = e.last_step_ms
+            for s in solvers:
+                s.fetch()
+        finally:
+            for s in solvers:
+                s.close()
+        runs[mode] = members
+    print("device ms for", NSTEPS - 1, "steps: batched", times[0], "persistent", times[1])
+    for c, a, b in zip(cases, runs[1], runs[0]):
+        fa, fb = a.fric(), b.fric()
+        rep = {"slip": _rel(fa[:, 70:73], fb[:, 70:73]), "slip_rate": _rel(fa[:, 73:76], fb[:, 73:76]),
+               "vel": _rel(a.arrays["velArr"], b.arrays["velArr"])}
+        assert all(v <= 1e-4 for v in rep.values()), rep
+        cpu = c.clone()
+        Oracle(cpu, nthreads()).step(NSTEPS)
+        err = _errors(cpu, a)
+        print("persistent member", c.sizes["nelem"], rep, "vs oracle", err)
+        _check(err)
+
+
+def test_persistent_launch_rejects_rate_and_state_members():
+    from eqdyna_gb300 import _native as N
+    from eqdyna_gb300.case import Case
+    from eqdyna_gb300.configs import config_c1
+    from eqdyna_gb300.solver import Ensemble, GpuSolver
+    case = Case.from_dir(config_c1(tempfile.mkdtemp(prefix="eqd_c1e_"), scale=8.0, nsteps=10))
+    solvers = [GpuSolver(case.clone(), precision="fp32", table_layout="records") for _ in range(2)]
+    try:
+        with Ensemble(solvers) as e:
+            with pytest.raises(N.EqdError) as ei:
+                e.set_mode(1)
+            assert ei.value.code == 5
+            e.step(3)  # the batched launches still run them
+    finally:
+        for s in solvers:
+            s.close()
