@@ -35,14 +35,16 @@ struct RecInterior {
   static constexpr int SLOT = 20;
   static_assert(N <= SLOT, "slot rows clear of the copied rows");
 };
-template <bool BODY, bool S0, int HG>
+// UNI (a group with one record): no record-index row, so the tile needs 512 bytes less shared
+// memory (the 8th CTA per SM on C1).
+template <bool BODY, bool S0, int HG, bool UNI = false>
 struct RecPml {
   static constexpr int REM = TabCommon<HG>::STR;
   static constexpr int RID = 0;                          // record index (u32): read again by the
-                                                         // node gather, so never overlaid
-  static constexpr int ABID = 1;                         // 2 rows of PML axis indices (u32)
-  static constexpr int STR = 3;                          // 15 split-field stress
-  static constexpr int ST0 = 18;                         // 6 initial stress
+                                                         // node gather, so never overlaid (not UNI)
+  static constexpr int ABID = UNI ? 0 : 1;               // 2 rows of PML axis indices (u32)
+  static constexpr int STR = ABID + 2;                   // 15 split-field stress
+  static constexpr int ST0 = STR + 15;                   // 6 initial stress
   static constexpr int N = ST0 + (S0 ? 6 : 0);
   static constexpr int ES = STR;                         // 6 split-stress sums over the stress rows
   static constexpr int FS = ES + 6;                      // 24 rows of per-corner forces (overlay)
@@ -162,7 +164,7 @@ __device__ __forceinline__ void interior_rec_body(const ElemArgs32 &a, int tile)
 
 template <bool BODY, bool S0, int HG, bool UNI>
 __device__ __forceinline__ void pml_rec_body(const ElemArgs32 &a, int tile) {
-  using L = RecPml<BODY, S0, HG>;
+  using L = RecPml<BODY, S0, HG, UNI>;
   using C = TabCommon<HG>;
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) unsigned long long bar;
@@ -185,7 +187,7 @@ __device__ __forceinline__ void pml_rec_body(const ElemArgs32 &a, int tile) {
     bulk_g2s(sinc, g.tile_inc + (size_t)tile * kTile * 8, 8 * kTile * 2, &bar);
     copy_rows(tab, L::STR, g.stress, 15, ld, e0, &bar);
     if (S0) copy_rows(tab, L::ST0, g.stress0, 6, ld, e0, &bar);
-    copy_rows(tab, L::RID, g.rec_id, 1, ld, e0, &bar);
+    if (!UNI) copy_rows(tab, L::RID, g.rec_id, 1, ld, e0, &bar);
     copy_rows(tab, L::ABID, g.ab_id, 2, ld, e0, &bar);
   }
   if (UNI && tid < 64) {

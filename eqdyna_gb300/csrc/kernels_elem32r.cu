@@ -114,12 +114,13 @@ int launch_interior(Context &c, cudaStream_t s, const ElemConst32 &k) {
 template <bool BODY, bool S0, int HG>
 int launch_pml(Context &c, cudaStream_t s, const ElemConst32 &k) {
   const ElemArgs32 a = elem_args(c, false, k);
-  const size_t sm = rec_smem<RecPml<BODY, S0, HG>>(a.g.max_tile_nodes);
   if (a.g.nrec == 1) {
+    const size_t sm = rec_smem<RecPml<BODY, S0, HG, true>>(a.g.max_tile_nodes);
     auto kern = elem_pml_rec<BODY, S0, HG, true>;
     if (allow_smem(kern, sm)) return EQD_ERR_CUDA;
     kern<<<a.g.ntiles, kTile, sm, s>>>(a);
   } else {
+    const size_t sm = rec_smem<RecPml<BODY, S0, HG>>(a.g.max_tile_nodes);
     auto kern = elem_pml_rec<BODY, S0, HG, false>;
     if (allow_smem(kern, sm)) return EQD_ERR_CUDA;
     kern<<<a.g.ntiles, kTile, sm, s>>>(a);
