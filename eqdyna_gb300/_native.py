@@ -80,7 +80,7 @@ TABLE_LAYOUTS = {"auto": 0, "streamed": 1, "records": 2}
 
 NEWTON_RECORD = 16
 MLP_PARAMS = 5313
-MLP_NORM = 18
+MLP_NORM = 34
 
 
 class MlpTrainOptions(C.Structure):

@@ -122,7 +122,7 @@ struct Context {
   int mlp_on = 0;
   float *mlp_p = nullptr;        // FP32 master parameters, gradients, Adam moments [kMlpParams]
   float *mlp_g = nullptr, *mlp_m = nullptr, *mlp_v = nullptr;
-  float mlp_norm[18] = {};       // in_shift[8], in_scale[8], out_shift, out_scale
+  float mlp_norm[34] = {};       // in_shift[8], in_scale[8], out_shift, out_scale, in_lo[8], in_hi[8]
   long long mlp_steps = 0;       // Adam steps taken
   // logged rate-and-state Newton solves (training data of the learned guess)
   double *nlog = nullptr;        // [nlog_steps][npair][16]

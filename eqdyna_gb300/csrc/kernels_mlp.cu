@@ -60,6 +60,8 @@ __device__ __forceinline__ void write_param(MlpDevice *m, int i, float v) {
   else m->b3 = v;
 }
 
+static_assert(kMlpNorm == EQD_MLP_NORM, "normalisation block of the C ABI");
+
 __global__ void mlp_sync_kernel(const float *__restrict__ P, MlpDevice *m, const float *__restrict__ norm) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < kMlpParams) write_param(m, i, P[i]);
@@ -71,6 +73,10 @@ __global__ void mlp_sync_kernel(const float *__restrict__ P, MlpDevice *m, const
   if (norm && i == 0) {
     m->out_shift = norm[16];
     m->out_scale = norm[17];
+  }
+  if (norm && i < 8) {
+    m->in_lo[i] = norm[18 + i];
+    m->in_hi[i] = norm[26 + i];
   }
 }
 
@@ -473,6 +479,17 @@ int mlp_train(Context &c, const eqd_mlp_train_options &o, float *epoch_loss, flo
     }
     const double nv = (double)valid.size();
     for (int k = 0; k < 8; ++k) norm[k] = 0.f, norm[8 + k] = 0.f;
+    // range of each raw feature over the training records: the guess is used inside it only
+    for (int k = 0; k < 8; ++k) norm[18 + k] = 0.f, norm[26 + k] = 0.f;
+    for (int k = 0; k < kMlpIn; ++k) {
+      float lo = hraw[(size_t)valid[0] * 8 + k], hi = lo;
+      for (const int r : valid) {
+        lo = std::min(lo, hraw[(size_t)r * 8 + k]);
+        hi = std::max(hi, hraw[(size_t)r * 8 + k]);
+      }
+      norm[18 + k] = lo;
+      norm[26 + k] = hi;
+    }
     for (int k = 0; k < 7; ++k) {
       const double mean = sum[k] / nv, var = std::max(sq[k] / nv - mean * mean, 0.0), sd = std::sqrt(var);
       const bool flat = sd <= 1e-7 * std::max(std::fabs(mean), 1e-30);

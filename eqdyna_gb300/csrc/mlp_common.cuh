@@ -23,7 +23,7 @@ constexpr int kMlpN3 = 8;    // output padded to one n8 tile (row 0 used)
 constexpr int kOffW1 = 0, kOffB1 = kOffW1 + kMlpH * kMlpK1, kOffW2 = kOffB1 + kMlpH;
 constexpr int kOffB2 = kOffW2 + kMlpH * kMlpH, kOffW3 = kOffB2 + kMlpH, kOffB3 = kOffW3 + kMlpH;
 constexpr int kMlpParams = kOffB3 + 1;
-constexpr int kMlpNorm = 2 * 8 + 2;  // in_shift[8], in_scale[8], out_shift, out_scale
+constexpr int kMlpNorm = 2 * 8 + 2 + 2 * 8;  // in_shift[8], in_scale[8], out_shift, out_scale, in_lo[8], in_hi[8]
 
 struct MlpDevice {
   __nv_bfloat16 W1[kMlpH * kMlpK1];  // [64][16], columns 6-15 zero
@@ -32,6 +32,7 @@ struct MlpDevice {
   float b1[kMlpH], b2[kMlpH], b3;
   float in_shift[8], in_scale[8];    // x = (f - shift) * scale
   float out_shift, out_scale;        // ln(V / V_trial) = y * scale + shift
+  float in_lo[8], in_hi[8];          // range of each raw feature over the training data
 };
 
 const void *mlp_device_params(Context &c);
@@ -152,7 +153,9 @@ __device__ __forceinline__ float mlp_eval_scalar(const MlpDevice &m, const float
 
 // Learned guess for each lane's solve.  `full` must be the same on all lanes of the warp and true
 // only when all 32 lanes are here; xs: 32 x 16 bf16 of shared scratch owned by this warp.  Returns
-// V_trial * exp(prediction), or V_trial when that is not a positive finite number.
+// V_trial * exp(prediction); V_trial itself (the plain guess) when that is not a positive finite
+// number, or when a feature of the solve lies outside its range over the training data (the model
+// would extrapolate).
 __device__ __forceinline__ double mlp_guess_warp(const MlpDevice &m, const float f[kMlpIn], double v0, bool full,
                                                  __nv_bfloat16 *xs) {
   float y;
@@ -187,8 +190,11 @@ __device__ __forceinline__ double mlp_guess_warp(const MlpDevice &m, const float
   } else {
     y = mlp_eval_scalar(m, f);
   }
+  bool inside = true;
+#pragma unroll
+  for (int i = 0; i < kMlpIn; ++i) inside = inside && f[i] >= m.in_lo[i] && f[i] <= m.in_hi[i];
   const double g = fmax(v0, 1e-30) * exp((double)(y * m.out_scale + m.out_shift));
-  return (g > 0.0 && isfinite(g)) ? g : v0;
+  return (inside && g > 0.0 && isfinite(g)) ? g : v0;
 }
 
 }  // namespace eqd

@@ -245,7 +245,9 @@ int eqd_gpu_newton_counts(eqd_context *ctx, int64_t out[5]);
 #define EQD_NEWTON_RECORD 16  /* doubles per logged solve: a b L V0 f0 fw Vw state0 fric(23)
                                  normal-traction trial-shear Tc fric(4) V_trial V iterations   */
 #define EQD_MLP_PARAMS 5313   /* FP32 parameters: W1[64][16] b1[64] W2[64][64] b2[64] W3[64] b3 */
-#define EQD_MLP_NORM 18       /* in_shift[8] in_scale[8] out_shift out_scale                     */
+#define EQD_MLP_NORM 34       /* in_shift[8] in_scale[8] out_shift out_scale in_lo[8] in_hi[8]:
+                                 the guess is used only for features inside [in_lo, in_hi], the
+                                 range of the training data; elsewhere the plain guess */
 
 typedef struct eqd_mlp_train_options {
   int32_t epochs;         /* passes over the training records                                  */

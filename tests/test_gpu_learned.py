@@ -125,3 +125,34 @@ def test_fast_and_reference_loops_take_the_same_decisions(c1_trained):
             assert np.array_equal(fast[k], ref[k]), k
         if not learned:
             assert kinds[2] > 0 and kinds[3] > 0
+
+
+def test_guess_outside_the_training_range_is_the_plain_guess(c1_trained):
+    """The learned guess is used only inside the range of each feature over the training data.
+    Solves logged later than the training data (here steps 161-280, into the rupture) whose
+    features leave that range are solved from the plain guess: the same slip rate and the same
+    iteration count as the plain replay.  Solves inside it still use the model."""
+    s, _, _ = c1_trained
+    params, norm = s.mlp_state()
+    lo, hi = norm[18:24].astype(np.float64), norm[26:32].astype(np.float64)
+    assert np.all(hi >= lo) and np.any(hi > lo)
+    s.newton_log(40, stride=3)
+    s.step(120)
+    rec = s.newton_records()
+    f = np.stack([np.log(np.maximum(rec[:, 13], 1e-30)), np.log(np.maximum(np.abs(rec[:, 7]), 1e-30)),
+                  rec[:, 9], rec[:, 10], rec[:, 0], rec[:, 1]], axis=1)
+    # the device compares binary32 features; the two logarithms may differ from numpy's in the last
+    # place, so those two get a margin on either side of the bound, the others are compared exactly
+    f32 = f.astype(np.float32).astype(np.float64)
+    margin = np.zeros(6)
+    margin[:2] = 1e-5 * np.maximum(np.abs(lo[:2]), np.abs(hi[:2]))
+    outside = np.any((f32 < lo - margin) | (f32 > hi + margin), axis=1)
+    inside = np.all((f32 >= lo + margin) & (f32 <= hi - margin), axis=1)
+    plain = s.replay_records(learned=False)
+    learned = s.replay_records(learned=True)
+    print("later solves:", len(rec), "outside the training range:", int(outside.sum()), "inside:", int(inside.sum()))
+    assert outside.sum() > 0
+    assert np.array_equal(learned["v"][outside], plain["v"][outside])
+    assert np.array_equal(learned["iters"][outside], plain["iters"][outside])
+    # inside the range the model drives the start: some solve takes another path than the plain one
+    assert np.any(learned["iters"][inside] != plain["iters"][inside])
