@@ -42,16 +42,21 @@ struct RecPml {
   static constexpr int REM = TabCommon<HG>::STR;
   static constexpr int RID = 0;                          // record index (u32): read again by the
                                                          // node gather, so never overlaid (not UNI)
-  static constexpr int ABID = UNI ? 0 : 1;               // 2 rows of PML axis indices (u32)
-  static constexpr int STR = ABID + 2;                   // 15 split-field stress
+  static constexpr int STR = UNI ? 0 : 1;                // 15 split-field stress
   static constexpr int ST0 = STR + 15;                   // 6 initial stress
   static constexpr int N = ST0 + (S0 ? 6 : 0);
   static constexpr int ES = STR;                         // 6 split-stress sums over the stress rows
   static constexpr int FS = ES + 6;                      // 24 rows of per-corner forces (overlay)
   static constexpr int NS = FS + 24;
+  // the slot table (built on the device) overlays force rows 20-23, clear of the copied rows: word
+  // column e holds element e's slots only, and each thread reads its slots before it writes its
+  // own forces there.  With the PML axis indices read from global memory by each element's thread
+  // (not copied), a tile needs 3 KB less shared memory than with both in rows of their own.
+  static constexpr int SLOT = FS + 20;
   static constexpr bool IDS = false;                     // node ids re-read by the gather: staging
-                                                         // them costs the 8th CTA per SM
+                                                         // them costs a CTA per SM
   static_assert(NS >= N, "copied rows fit");
+  static_assert(SLOT >= N, "slot rows clear of the copied rows");
 };
 
 template <class L>
@@ -174,7 +179,8 @@ __device__ __forceinline__ void pml_rec_body(const ElemArgs32 &a, int tile) {
   const ElemGroup<float> &g = a.g;
   const int Mmax = g.max_tile_nodes;
   float *tab = reinterpret_cast<float *>(smem);
-  const TileSmem ts = tile_smem(tab + L::NS * kTile, Mmax, L::IDS);
+  const TileSmem ts = tile_smem(tab + L::NS * kTile, Mmax, L::IDS,
+                                reinterpret_cast<unsigned short *>(tab + L::SLOT * kTile));
   unsigned short *sinc = ts.sinc, *slot_of = ts.slot_of;
   float *sv = ts.sv, *sd = ts.sd;
   const int tid = threadIdx.x;
@@ -188,7 +194,6 @@ __device__ __forceinline__ void pml_rec_body(const ElemArgs32 &a, int tile) {
     copy_rows(tab, L::STR, g.stress, 15, ld, e0, &bar);
     if (S0) copy_rows(tab, L::ST0, g.stress0, 6, ld, e0, &bar);
     if (!UNI) copy_rows(tab, L::RID, g.rec_id, 1, ld, e0, &bar);
-    copy_rows(tab, L::ABID, g.ab_id, 2, ld, e0, &bar);
   }
   if (UNI && tid < 64) {
     const int ca = tid >> 3, k = tid & 7;
@@ -211,7 +216,7 @@ __device__ __forceinline__ void pml_rec_body(const ElemArgs32 &a, int tile) {
   int sl[8];
   load_slots(slot_of, tid, sl);
   if (tid < live) {
-    const unsigned ab01 = row_u32(tab, L::ABID, tid), ab2 = row_u32(tab, L::ABID + 1, tid);
+    const unsigned ab01 = __ldg(g.ab_id + e), ab2 = __ldg(g.ab_id + (size_t)ld + e);
     if (UNI) {
       const UniSrc<L> S{a.rp, tab, tid, g.ab_tab, g.ab_stride, ab01, ab2};
       pml_element<BODY, S0, HG>(S, sv, sd, Mmax, sl, tid, a.k, g.stress + e, (size_t)ld, es, cfh);
