@@ -183,6 +183,8 @@ def gpu_lib():
         lib.eqd_gpu_element_tables.restype = C.c_int
         lib.eqd_gpu_check_conversions.argtypes = [C.c_int32, C.c_int64, C.c_uint64, C.POINTER(C.c_int64)]
         lib.eqd_gpu_check_conversions.restype = C.c_int
+        lib.eqd_gpu_wait_selftest.argtypes = [C.c_int32, C.c_int32, C.POINTER(C.c_int32), d_p]
+        lib.eqd_gpu_wait_selftest.restype = C.c_int
         lib.eqd_gpu_fetch_fric_rows.argtypes = [C.c_void_p, C.POINTER(C.c_int32), C.c_int32, d_p]
         lib.eqd_gpu_fetch_fric_rows.restype = C.c_int
         lib.eqd_gpu_step_async.argtypes = [C.c_void_p, C.c_int32, C.c_int32]
@@ -238,7 +240,7 @@ GPU_SYMBOLS = ["eqd_gpu_init", "eqd_gpu_step", "eqd_gpu_fetch", "eqd_gpu_fetch_f
                "eqd_gpu_newton_log", "eqd_gpu_newton_records", "eqd_gpu_mlp_train", "eqd_gpu_mlp_get",
                "eqd_gpu_mlp_set", "eqd_gpu_mlp_enable", "eqd_gpu_newton_replay", "eqd_mlp_gradient",
                "eqd_gpu_newton_replay_records", "eqd_gpu_element_tables",
-               "eqd_gpu_fp64_fma_peak", "eqd_gpu_check_conversions", "eqd_gpu_elem_forces_noalloc"]
+               "eqd_gpu_fp64_fma_peak", "eqd_gpu_check_conversions", "eqd_gpu_wait_selftest", "eqd_gpu_elem_forces_noalloc"]
 CASE_SYMBOLS = ["eqd_case_build", "eqd_case_build_opt", "eqd_case_view", "eqd_case_array_len", "eqd_case_dims",
                 "eqd_case_lines", "eqd_case_phase_seconds", "eqd_case_free", "eqd_case_last_error"]
 

@@ -242,6 +242,17 @@ double live_fraction(const ElemBins &b, int bx, int by, int bz, int tile) {
 // also tries bins by rank (bins_by_rank) and bricks a little smaller than the tuned one, and keeps
 // the candidate with the most live slots.  Returns the live fraction chosen (0 when the order
 // could not be built).
+// Every node id of the connectivity in 1 .. nnode: checked before anything reads coordinates or
+// builds tables through it (a bad id would index past the caller's arrays).
+bool connectivity_in_range(const eqd_host_arrays &a) {
+  const long long n8 = 8 * (long long)a.nelem;
+  const int nn = a.nnode;
+  int bad = 0;
+#pragma omp parallel for schedule(static) reduction(| : bad)
+  for (long long q = 0; q < n8; ++q) bad |= (a.nodeElemIdRelation[q] < 1 || a.nodeElemIdRelation[q] > nn);
+  return !bad;
+}
+
 double brick_order(const eqd_host_arrays &a, std::vector<int> &ids, int bx, int bz, int by, int tile) {
   const size_t m = ids.size();
   if (m == 0) return 1.0;
@@ -574,12 +585,11 @@ int build_device_state(eqd_context &X, const eqd_scalars &s, const eqd_host_arra
   // Without host tables the element tables and nodal masses are built on the device from the mesh
   // (setup_device.cu), bit for bit the host's: a node's mass is the value of each of its equations
   // in nodalMassArr and its fnms.
+  if (!connectivity_in_range(a)) return EQD_ERR_INPUT;
   const bool dev_tables = a.eleshp == nullptr;
   std::unique_ptr<DeviceMesh> dmesh;
   std::vector<double> dev_mass;
   if (dev_tables) {
-    for (long long q = 0; q < 8 * (long long)ne; ++q)
-      if (a.nodeElemIdRelation[q] < 1 || a.nodeElemIdRelation[q] > nn) return EQD_ERR_INPUT;
     dmesh.reset(new DeviceMesh());
     RC(dmesh->upload(a));
     RC(device_nodal_mass(a, *dmesh, dev_mass));
@@ -2153,8 +2163,9 @@ int eqd_gpu_fp64_fma_peak(int32_t device, double *tflops) {
 int eqd_host_element_order(const eqd_host_arrays *a, int32_t group, int32_t tile_shape, int32_t *out,
                            int64_t cap, int64_t *n_out, double *live) {
   if (!a || !n_out || (group != 0 && group != 1) || a->nelem < 0 || !a->elemTypeArr ||
-      !a->nodeElemIdRelation || !a->meshCoor)
+      !a->nodeElemIdRelation || !a->meshCoor || a->nnode <= 0)
     return EQD_ERR_INPUT;
+  if (!connectivity_in_range(*a)) return EQD_ERR_INPUT;
   std::vector<int> ids;
   for (int e = 0; e < a->nelem; ++e) {
     const int t = a->elemTypeArr[e];

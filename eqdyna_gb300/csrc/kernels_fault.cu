@@ -1182,6 +1182,78 @@ __global__ void fpconv_check_kernel(long long n, unsigned long long seed, unsign
 
 }  // namespace eqd
 
+namespace eqd {
+namespace {
+// Self-tests of the bounded waits: a completion that never comes must make the wait give up and
+// flag bit 2 of the error word, not hang.
+__global__ void wait_selftest_mbar(int *err) {
+  __shared__ __align__(8) unsigned long long bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    mbar_expect_tx(&bar, 16u);  // 16 bytes that no copy delivers
+  }
+  __syncthreads();
+  mbar_wait_bounded(&bar, err);
+}
+__global__ void wait_selftest_grid(unsigned *bar, int *err) {
+  if (blockIdx.x == 1) return;  // this CTA leaves without arriving at the barrier
+  grid_barrier(bar, err);
+}
+}  // namespace
+}  // namespace eqd
+
+extern "C" int eqd_gpu_wait_selftest(int32_t device, int32_t which, int32_t *status, double *ms) {
+  using namespace eqd;
+  if (!status || (which != 0 && which != 1)) return EQD_ERR_INPUT;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return EQD_ERR_NO_DEVICE;
+  }
+  EQD_CUDA_OK(cudaSetDevice(device));
+  if (which == 1) {
+    int coop = 0;
+    EQD_CUDA_OK(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device));
+    if (!coop) return EQD_ERR_UNSUPPORTED;
+  }
+  int *err = nullptr;
+  unsigned *bar = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  int rc = EQD_OK;
+  if (cudaMalloc(&err, sizeof(int)) != cudaSuccess || cudaMalloc(&bar, 2 * sizeof(unsigned)) != cudaSuccess ||
+      cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+    cudaGetLastError();
+    rc = EQD_ERR_OOM;
+  }
+  if (!rc) {
+    cudaMemset(err, 0, sizeof(int));
+    cudaMemset(bar, 0, 2 * sizeof(unsigned));
+    cudaEventRecord(e0);
+    if (which == 0) {
+      wait_selftest_mbar<<<1, 32>>>(err);
+    } else {
+      void *args[] = {&bar, &err};
+      if (cudaLaunchCooperativeKernel(reinterpret_cast<const void *>(wait_selftest_grid), dim3(2), dim3(32), args, 0,
+                                      nullptr) != cudaSuccess)
+        rc = EQD_ERR_CUDA;
+    }
+    cudaEventRecord(e1);
+    int h = 0;
+    if (!rc && (cudaEventSynchronize(e1) != cudaSuccess ||
+                cudaMemcpy(&h, err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess))
+      rc = EQD_ERR_CUDA;
+    float t = 0.f;
+    if (!rc) cudaEventElapsedTime(&t, e0, e1);
+    if (ms) *ms = t;
+    *status = (h & 2) ? EQD_ERR_TIMEOUT : EQD_OK;
+  }
+  if (err) cudaFree(err);
+  if (bar) cudaFree(bar);
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  return rc;
+}
+
 extern "C" int eqd_gpu_check_conversions(int32_t device, int64_t n, uint64_t seed, int64_t mismatches[2]) {
   using namespace eqd;
   if (n <= 0 || !mismatches) return EQD_ERR_INPUT;

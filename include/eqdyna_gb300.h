@@ -358,6 +358,14 @@ int eqd_host_element_order(const eqd_host_arrays *a, int32_t group, int32_t tile
 int eqd_gpu_element_tables(int32_t device, const eqd_host_arrays *a, double *eleshp, double *eledet,
                            double *elemass, double *ss, double *phi, double *nodalMassArr, double *fnms);
 
+/* No counterpart in the reference: a self-test of the failure path of the library's device-side
+ * waits.  which = 0 arms an mbarrier (the kind each element tile waits on for its bulk copies) for
+ * bytes that no copy delivers; which = 1 runs the persistent ensemble kernel's grid barrier with
+ * one of two CTAs leaving without arriving.  The bounded wait must give up (after about 0.2 s and
+ * 2 s) and flag the error word: *status = EQD_ERR_TIMEOUT, *ms = the kernel's duration.  Nothing
+ * faults or hangs, and the device stays usable. */
+int eqd_gpu_wait_selftest(int32_t device, int32_t which, int32_t *status, double *ms);
+
 /* Measured binary64 fused-multiply-add throughput of a device (TFLOP/s, 2 flops per FMA),
  * from a register-resident FMA chain kernel; used as the compute roofline of the FP64 form. */
 int eqd_gpu_fp64_fma_peak(int32_t device, double *tflops);

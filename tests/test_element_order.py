@@ -112,3 +112,20 @@ def test_rejects_bad_arguments(c3_case):
     rc = lib.eqd_host_element_order(C.byref(ha), 1, 0, small.ctypes.data_as(C.POINTER(C.c_int32)), 4,
                                     C.byref(n), C.byref(live))
     assert rc != 0 and n.value > 4
+
+
+def test_node_id_out_of_range_is_rejected_before_any_coordinate_is_read(c3_case):
+    """The element order reads the coordinates of every element's nodes; a connectivity with a node
+    id outside 1 .. nnode (here one past the end, and a 0-based 0) is refused first (EQD_ERR_INPUT)
+    rather than read past the caller's coordinate array.  eqd_gpu_init makes the same check
+    before anything else."""
+    from eqdyna_gb300 import _native as N
+    lib = N.gpu_lib()
+    for bad_id in (c3_case.sizes["nnode"] + 1, 0):
+        case = c3_case.clone()
+        conn = case.arrays["nodeElemIdRelation"].copy()
+        conn[8 * 5 + 2] = bad_id
+        case.arrays["nodeElemIdRelation"] = conn
+        ha = case.host_arrays()
+        n, live = C.c_int64(), C.c_double()
+        assert lib.eqd_host_element_order(C.byref(ha), 0, 0, None, 0, C.byref(n), C.byref(live)) == 1
