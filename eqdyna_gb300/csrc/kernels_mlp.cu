@@ -2,10 +2,11 @@
 // backward, Adam), replay of logged solves, and the model's device parameter block.
 //
 // Training data are the rate-and-state Newton solves the plain method itself performs
-// (eqd_gpu_newton_log).  Every kernel that touches the MLP runs its matrix products on the tensor
-// cores with mma.sync.m16n8k16 (bf16 operands, fp32 accumulation; fragment helpers in
-// mlp_common.cuh); biases, losses, Adam and the rank-1 output layer's gradient are fp32 on the
-// CUDA cores.
+// (eqd_gpu_newton_log).  Training runs its products on the 5th-generation tensor cores
+// (tcgen05.mma with accumulators in tensor memory, tcgen05.cuh), 128 samples per CTA; inference
+// inside the fault and replay kernels is warp-cooperative (mma.sync.m16n8k16, mlp_common.cuh).
+// Both use bf16 operands and fp32 accumulation; biases, losses, Adam and the rank-1 output layer
+// are fp32 on the CUDA cores.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -15,12 +16,13 @@
 #include "eqd_device.cuh"
 #include "mlp_common.cuh"
 #include "rsf_newton.cuh"
+#include "tcgen05.cuh"
 
 namespace eqd {
 
 namespace {
 
-constexpr int kTrainRows = 64;  // samples per CTA (4 warps x 16)
+constexpr int kTrainRows = 128;  // samples per CTA = threads = the M of every tensor-core product
 
 // ---- records -> raw features ---------------------------------------------------------------------
 // raw[r][0..5] features, [6] target ln(V / V_trial), [7] 1 if finite
@@ -97,13 +99,6 @@ __global__ void mlp_adam_kernel(float *__restrict__ P, float *__restrict__ G, fl
   write_param(m, i, p);
 }
 
-__device__ __forceinline__ void to_a(unsigned a[4], const float lo[4], const float hi[4]) {
-  a[0] = pack_bf16(lo[0], lo[1]);
-  a[1] = pack_bf16(lo[2], lo[3]);
-  a[2] = pack_bf16(hi[0], hi[1]);
-  a[3] = pack_bf16(hi[2], hi[3]);
-}
-
 struct TrainBatch {
   const __nv_bfloat16 *X;  // [n][16]
   const float *Y;          // [n]
@@ -112,191 +107,254 @@ struct TrainBatch {
   float inv_count;         // 1 / samples in the batch
 };
 
-// Forward + backward of one batch, 64 samples per CTA: loss += sum (y - t)^2 / (2 count),
-// G += d loss / d params.  Weight gradients contract over the CTA's samples on the tensor cores
-// (transposed activations staged in shared memory) and are reduced across CTAs with fp32 atomics.
-__global__ void __launch_bounds__(128) mlp_grad_kernel(const MlpDevice *__restrict__ m, TrainBatch tb,
-                                                       float *__restrict__ G, float *__restrict__ loss) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  __nv_bfloat16 *sW1 = reinterpret_cast<__nv_bfloat16 *>(smem);  // [64][16]
-  __nv_bfloat16 *sW2 = sW1 + kMlpH * kMlpK1;                     // [64][64]
-  __nv_bfloat16 *sW2T = sW2 + kMlpH * kMlpH;                     // [64][64] transposed
-  __nv_bfloat16 *sW3 = sW2T + kMlpH * kMlpH;                     // [8][64]
-  __nv_bfloat16 *XT = sW3 + kMlpN3 * kMlpH;                      // [16][64 samples]
-  __nv_bfloat16 *H1T = XT + kMlpK1 * kTrainRows;                 // [64][64 samples]
-  __nv_bfloat16 *dZ2T = H1T + kMlpH * kTrainRows;
-  __nv_bfloat16 *dZ1T = dZ2T + kMlpH * kTrainRows;
-  float *sb1 = reinterpret_cast<float *>(dZ1T + kMlpH * kTrainRows);
-  float *sb2 = sb1 + kMlpH;
-  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5, g = lane >> 2, t = lane & 3;
-  for (int k = tid; k < kMlpH * kMlpK1; k += blockDim.x) sW1[k] = m->W1[k];
-  for (int k = tid; k < kMlpH * kMlpH; k += blockDim.x) {
-    sW2[k] = m->W2[k];
-    sW2T[(k % kMlpH) * kMlpH + k / kMlpH] = m->W2[k];
+// Shared memory of the training kernel: the tensor-core operands (bf16, tc::kmaj_off layout), then
+// the fp32 bias / output-weight rows, the mbarrier and the tensor-memory address.
+struct GradSmem {
+  static constexpr int W1 = 0;                                   // B of Z1: [64 n1][16 k]
+  static constexpr int W2 = W1 + kMlpH * kMlpK1 * 2;             // B of Z2: [64 n2][64 k1]
+  static constexpr int W2T = W2 + kMlpH * kMlpH * 2;             // B of dH1: [64 k1][64 n2]
+  static constexpr int X = W2T + kMlpH * kMlpH * 2;              // A of Z1: [128 s][16 k]
+  static constexpr int AT = X + kTrainRows * kMlpK1 * 2;         // A of dW: [64 n2 | 64 n1][128 s]
+  static constexpr int H1 = AT + 2 * kMlpH * kTrainRows * 2;     // A of Z2: [128 s][64 k1]
+  static constexpr int DZ2 = H1 + kTrainRows * kMlpH * 2;        // A of dH1: [128 s][64 n2]
+  static constexpr int BT = DZ2 + kTrainRows * kMlpH * 2;        // B of dW: [64 k1 | 16 k][128 s]
+  static constexpr int VEC = BT + (kMlpH + kMlpK1) * kTrainRows * 2;  // b1[64], b2[64], w3[64] fp32
+  static constexpr int BAR = VEC + 3 * kMlpH * 4;
+  static constexpr int TMEM = BAR + 8;
+  static constexpr int BYTES = TMEM + 8;
+};
+// 2 CTAs per SM at most (3 x 108 KB exceed the SM's shared memory), so the 2 x kGradCols columns
+// they allocate never exceed the SM's 512 and the allocation never waits.
+constexpr uint32_t kGradCols = 256;
+static_assert(GradSmem::BYTES > 228 * 1024 / 3, "the shared memory must keep a third CTA off the SM");
+static_assert(2 * kGradCols <= 512, "tensor memory of two CTAs");
+
+// Forward + backward of one batch, kTrainRows = 128 samples per CTA (thread i owns sample i, which is
+// row / tensor-memory lane i of every product): loss += sum (y - t)^2 / (2 count), G += d loss /
+// d params.  The four products run on the 5th-generation tensor cores (tcgen05.mma, kind::f16, bf16
+// operands from shared memory, fp32 accumulators in tensor memory), issued by thread 0:
+//   Z1 = X W1^T (cols 0-63), Z2 = H1 W2^T (cols 64-127), dH1 = dZ2 W2 (cols 128-191),
+//   [dW2 | . ; . | dW1] = [dZ2^T ; dZ1^T] [H1 | X] over the CTA's samples (cols 0-79, M 128, N 80).
+// Biases, ReLU, the rank-1 output layer and its error are fp32 on the CUDA cores; the bias and
+// output-weight gradients are column sums over the CTA's rows; all gradients reach G by fp32
+// atomics.  Every wait is bounded: on a timeout bit 2 of *err is set and the CTA frees its tensor
+// memory and returns.
+__global__ void __launch_bounds__(kTrainRows, 1) mlp_grad_kernel(const MlpDevice *__restrict__ m, TrainBatch tb,
+                                                                 float *__restrict__ G, float *__restrict__ loss,
+                                                                 int *__restrict__ err) {
+  using S = GradSmem;
+  extern __shared__ __align__(128) unsigned char smem[];
+  float *sb1 = reinterpret_cast<float *>(smem + S::VEC), *sb2 = sb1 + kMlpH, *sw3 = sb2 + kMlpH;
+  unsigned long long *bar = reinterpret_cast<unsigned long long *>(smem + S::BAR);
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(smem + S::TMEM);
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  auto st16 = [&](int off, const uint4 &v) { *reinterpret_cast<uint4 *>(smem + off) = v; };
+  auto st2 = [&](int off, __nv_bfloat16 v) { *reinterpret_cast<__nv_bfloat16 *>(smem + off) = v; };
+
+  if (w == 0) tc::tmem_alloc(tslot, kGradCols);
+  if (tid == 0) e32::mbar_init(bar, 1);
+  // weights (16-byte rows of 8 bf16), the transposed W2, biases and the output row
+  {
+    const uint4 *w1 = reinterpret_cast<const uint4 *>(m->W1);  // [64][16] = 2 chunks per row
+    st16(S::W1 + tc::kmaj_off(tid >> 1, 8 * (tid & 1), kMlpK1), w1[tid]);
+    const uint4 *w2 = reinterpret_cast<const uint4 *>(m->W2);  // [64][64] = 8 chunks per row
+    for (int q = tid; q < kMlpH * 8; q += kTrainRows) st16(S::W2 + tc::kmaj_off(q >> 3, 8 * (q & 7), kMlpH), w2[q]);
+    for (int q = tid; q < kMlpH * kMlpH; q += kTrainRows) {
+      const int n2 = q >> 6, k1 = q & 63;
+      st2(S::W2T + tc::kmaj_off(k1, n2, kMlpH), m->W2[q]);
+    }
+    if (tid < kMlpH) {
+      sb1[tid] = m->b1[tid];
+      sb2[tid] = m->b2[tid];
+      sw3[tid] = __bfloat162float(m->W3[tid]);
+    }
   }
-  for (int k = tid; k < kMlpN3 * kMlpH; k += blockDim.x) sW3[k] = m->W3[k];
-  for (int k = tid; k < kMlpH; k += blockDim.x) sb1[k] = m->b1[k], sb2[k] = m->b2[k];
+  // this thread's sample: X row (zero past the batch) into X and, transposed, rows 64-79 of BT
+  const long long q = tb.start + (long long)blockIdx.x * kTrainRows + tid;
+  const bool valid = q < tb.start + tb.count;
+  const long long sid = valid ? (tb.order ? (long long)tb.order[q] : q) : -1;
+  {
+    uint4 x0 = make_uint4(0u, 0u, 0u, 0u), x1 = x0;
+    if (valid) {
+      const uint4 *xr = reinterpret_cast<const uint4 *>(tb.X + sid * kMlpK1);
+      x0 = xr[0];
+      x1 = xr[1];
+    }
+    st16(S::X + tc::kmaj_off(tid, 0, kMlpK1), x0);
+    st16(S::X + tc::kmaj_off(tid, 8, kMlpK1), x1);
+    const __nv_bfloat16 *e0 = reinterpret_cast<const __nv_bfloat16 *>(&x0);
+    const __nv_bfloat16 *e1 = reinterpret_cast<const __nv_bfloat16 *>(&x1);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      st2(S::BT + tc::kmaj_off(kMlpH + k, tid, kTrainRows), e0[k]);
+      st2(S::BT + tc::kmaj_off(kMlpH + 8 + k, tid, kTrainRows), e1[k]);
+    }
+  }
+  const float target = valid ? tb.Y[sid] : 0.f;
+  tc::fence_smem_to_async();
+  tc::fence_before_sync();
   __syncthreads();
-  const float b3 = m->b3;
-  const int s0 = w * 16;
-  const long long base = tb.start + (long long)blockIdx.x * kTrainRows + s0;
-  const long long end = tb.start + tb.count;
-  auto sid = [&](int r) -> long long {
-    const long long q = base + r;
-    if (q >= end) return -1;
-    return tb.order ? (long long)tb.order[q] : q;
+  tc::fence_after_sync();
+  const uint32_t tmem = *tslot;
+  const uint32_t trow = tmem + ((uint32_t)(32 * w) << 16);  // this warp's lanes
+  const uint32_t id64 = tc::idesc_bf16_f32(128, 64), id80 = tc::idesc_bf16_f32(128, 80);
+  unsigned phase = 0;
+  bool ok = true;
+  // issue, commit, and wait for one group of MMAs; false (on every thread) after a timeout
+  auto run = [&](auto issue) -> bool {
+    if (tid == 0) {
+      issue();
+      tc::commit(bar);
+    }
+    bool done = tc::mbar_wait_parity(bar, phase);
+    if (!done) {
+      atomicOr(err, 2);
+      done = tc::mbar_wait_parity(bar, phase);  // let the MMAs end before the memory is freed
+    }
+    phase ^= 1u;
+    tc::fence_after_sync();
+    return __syncthreads_and(done) != 0;
   };
-  const long long ig = sid(g), ig8 = sid(g + 8);
-  unsigned xa[4] = {0u, 0u, 0u, 0u};
-  if (ig >= 0) {
-    xa[0] = ld32(tb.X + ig * kMlpK1 + 2 * t);
-    xa[2] = ld32(tb.X + ig * kMlpK1 + 8 + 2 * t);
-  }
-  if (ig8 >= 0) {
-    xa[1] = ld32(tb.X + ig8 * kMlpK1 + 2 * t);
-    xa[3] = ld32(tb.X + ig8 * kMlpK1 + 8 + 2 * t);
-  }
-  {  // X^T for the first layer's weight gradient
-    const __nv_bfloat16 *e = reinterpret_cast<const __nv_bfloat16 *>(xa);
-    XT[(2 * t) * kTrainRows + s0 + g] = e[0];
-    XT[(2 * t + 1) * kTrainRows + s0 + g] = e[1];
-    XT[(2 * t) * kTrainRows + s0 + g + 8] = e[2];
-    XT[(2 * t + 1) * kTrainRows + s0 + g + 8] = e[3];
-    XT[(8 + 2 * t) * kTrainRows + s0 + g] = e[4];
-    XT[(9 + 2 * t) * kTrainRows + s0 + g] = e[5];
-    XT[(8 + 2 * t) * kTrainRows + s0 + g + 8] = e[6];
-    XT[(9 + 2 * t) * kTrainRows + s0 + g + 8] = e[7];
-  }
-  float z1[8][4], z2[8][4], out[4];
-  mlp_forward16(xa, sW1, sW2, sW3, sb1, sb2, b3, z1, z2, out);
-  // output error on the lanes that hold column 0
-  float d0 = 0.f, d2 = 0.f;
-  if (t == 0) {
-    if (ig >= 0) d0 = out[0] - tb.Y[ig];
-    if (ig8 >= 0) d2 = out[2] - tb.Y[ig8];
-  }
-  float lsum = (d0 * d0 + d2 * d2) * 0.5f * tb.inv_count;
-  const float dg = __shfl_sync(0xffffffffu, d0 * tb.inv_count, lane & ~3);
-  const float dg8 = __shfl_sync(0xffffffffu, d2 * tb.inv_count, lane & ~3);
-  // layer 3 and 2 backward
-  float dz2[8][4], gw3[8][2], gb2[8][2];
+
+  // ---- Z1 = X W1^T -----------------------------------------------------------------------------
+  ok = run([&] { tc::mma_bf16(tmem + 0, tc::kmaj_desc(smem + S::X, kMlpK1, 0), tc::kmaj_desc(smem + S::W1, kMlpK1, 0), id64, false); });
+  if (ok) {
+    // H1 = bf16(relu(Z1 + b1)) as the A rows of Z2 and, transposed, rows 0-63 of BT
 #pragma unroll
-  for (int j = 0; j < 8; ++j)
+    for (int c = 0; c < kMlpH / 16; ++c) {
+      float z[16];
+      tc::tmem_ld16(trow + 16 * c, z);
+      __align__(16) __nv_bfloat16 h[16];
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const int n = 8 * j + 2 * t + (q & 1);
-      const float dv = q < 2 ? dg : dg8;
-      const float h2 = bf16r(fmaxf(z2[j][q], 0.f));
-      dz2[j][q] = z2[j][q] > 0.f ? dv * __bfloat162float(sW3[n]) : 0.f;
-      if (q < 2) gw3[j][q] = dv * h2, gb2[j][q] = dz2[j][q];
-      else gw3[j][q - 2] += dv * h2, gb2[j][q - 2] += dz2[j][q];
+      for (int i = 0; i < 16; ++i) h[i] = __float2bfloat16(fmaxf(z[i] + sb1[16 * c + i], 0.f));
+      st16(S::H1 + tc::kmaj_off(tid, 16 * c, kMlpH), *reinterpret_cast<const uint4 *>(h));
+      st16(S::H1 + tc::kmaj_off(tid, 16 * c + 8, kMlpH), *reinterpret_cast<const uint4 *>(h + 8));
+#pragma unroll
+      for (int i = 0; i < 16; ++i) st2(S::BT + tc::kmaj_off(16 * c + i, tid, kTrainRows), h[i]);
     }
-  // dH1 = dZ2 W2 (tensor cores, B = W2 read transposed), then dZ1
-  float dz1[8][4];
-#pragma unroll
-  for (int j = 0; j < 8; ++j) dz1[j][0] = dz1[j][1] = dz1[j][2] = dz1[j][3] = 0.f;
-#pragma unroll
-  for (int kk = 0; kk < 4; ++kk) {
-    unsigned a[4];
-    to_a(a, dz2[2 * kk], dz2[2 * kk + 1]);
-#pragma unroll
-    for (int j = 0; j < 8; ++j) {
-      unsigned b[2];
-      frag_bt(b, sW2T, kMlpH, 8 * j, 16 * kk);
-      mma_bf16(dz1[j], a, b);
-    }
+    tc::fence_smem_to_async();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    // ---- Z2 = H1 W2^T ----------------------------------------------------------------------------
+    ok = run([&] {
+      for (int kk = 0; kk < kMlpH / 16; ++kk)
+        tc::mma_bf16(tmem + 64, tc::kmaj_desc(smem + S::H1, kMlpH, kk), tc::kmaj_desc(smem + S::W2, kMlpH, kk), id64,
+                     kk > 0);
+    });
   }
-  float gb1[8][2];
+  if (ok) {
+    // output y = relu(Z2 + b2) . w3 + b3 (bf16 activations), its error, dZ2 = (z2 > 0) dy w3; Z2 is
+    // read from tensor memory twice rather than held in registers
+    float y = m->b3;
 #pragma unroll
-  for (int j = 0; j < 8; ++j)
+    for (int c = 0; c < kMlpH / 16; ++c) {
+      float z[16];
+      tc::tmem_ld16(trow + 64 + 16 * c, z);
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      dz1[j][q] = z1[j][q] > 0.f ? dz1[j][q] : 0.f;
-      if (q < 2) gb1[j][q] = dz1[j][q];
-      else gb1[j][q - 2] += dz1[j][q];
+      for (int i = 0; i < 16; ++i) y = fmaf(sw3[16 * c + i], bf16r(fmaxf(z[i] + sb2[16 * c + i], 0.f)), y);
     }
-  // transposed activations / errors of this warp's 16 samples
+    const float d = valid ? y - target : 0.f;
+    const float dy = d * tb.inv_count;
+    float lsum = d * d * 0.5f * tb.inv_count, db3 = dy;
 #pragma unroll
-  for (int j = 0; j < 8; ++j)
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const int n = 8 * j + 2 * t + (q & 1), r = s0 + g + (q < 2 ? 0 : 8);
-      H1T[n * kTrainRows + r] = __float2bfloat16(fmaxf(z1[j][q], 0.f));
-      dZ2T[n * kTrainRows + r] = __float2bfloat16(dz2[j][q]);
-      dZ1T[n * kTrainRows + r] = __float2bfloat16(dz1[j][q]);
+    for (int o = 16; o >= 1; o >>= 1) {
+      lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
+      db3 += __shfl_xor_sync(0xffffffffu, db3, o);
     }
-  // column sums over the warp's rows: reduce across the 8 row groups (lane bits 2-4)
+    if (lane == 0) {
+      atomicAdd(loss, lsum);
+      atomicAdd(G + kOffB3, db3);
+    }
 #pragma unroll
-  for (int j = 0; j < 8; ++j)
+    for (int h = 0; h < 2; ++h) {  // 32 columns at a time
+      float gw3[32], gb2[32];
 #pragma unroll
-    for (int q = 0; q < 2; ++q) {
+      for (int c = 0; c < 2; ++c) {
+        float z[16];
+        tc::tmem_ld16(trow + 64 + 32 * h + 16 * c, z);
+        __align__(16) __nv_bfloat16 e[16];
 #pragma unroll
-      for (int o = 4; o < 32; o <<= 1) {
-        gw3[j][q] += __shfl_xor_sync(0xffffffffu, gw3[j][q], o);
-        gb2[j][q] += __shfl_xor_sync(0xffffffffu, gb2[j][q], o);
-        gb1[j][q] += __shfl_xor_sync(0xffffffffu, gb1[j][q], o);
+        for (int i = 0; i < 16; ++i) {
+          const int j = 32 * h + 16 * c + i;
+          const float z2 = z[i] + sb2[j];
+          const float dz = z2 > 0.f ? dy * sw3[j] : 0.f;
+          gw3[16 * c + i] = dy * bf16r(fmaxf(z2, 0.f));
+          gb2[16 * c + i] = dz;
+          e[i] = __float2bfloat16(dz);
+          st2(S::AT + tc::kmaj_off(j, tid, kTrainRows), e[i]);
+        }
+        st16(S::DZ2 + tc::kmaj_off(tid, 32 * h + 16 * c, kMlpH), *reinterpret_cast<const uint4 *>(e));
+        st16(S::DZ2 + tc::kmaj_off(tid, 32 * h + 16 * c + 8, kMlpH), *reinterpret_cast<const uint4 *>(e + 8));
       }
-      if (g == 0) {
-        const int n = 8 * j + 2 * t + q;
-        atomicAdd(G + kOffW3 + n, gw3[j][q]);
-        atomicAdd(G + kOffB2 + n, gb2[j][q]);
-        atomicAdd(G + kOffB1 + n, gb1[j][q]);
-      }
+      const float a = tc::warp_column_sums32(gw3), b = tc::warp_column_sums32(gb2);
+      atomicAdd(G + kOffW3 + 32 * h + lane, a);
+      atomicAdd(G + kOffB2 + 32 * h + lane, b);
     }
-  float db3 = (t == 0) ? (d0 + d2) * tb.inv_count : 0.f;
+    tc::fence_smem_to_async();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    // ---- dH1 = dZ2 W2 ----------------------------------------------------------------------------
+    ok = run([&] {
+      for (int kk = 0; kk < kMlpH / 16; ++kk)
+        tc::mma_bf16(tmem + 128, tc::kmaj_desc(smem + S::DZ2, kMlpH, kk), tc::kmaj_desc(smem + S::W2T, kMlpH, kk),
+                     id64, kk > 0);
+    });
+  }
+  if (ok) {
+    // dZ1 = (z1 > 0) dH1: rows 64-127 of AT (transposed) and the b1 column sums
 #pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    db3 += __shfl_xor_sync(0xffffffffu, db3, o);
-    lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
+    for (int h = 0; h < 2; ++h) {
+      float gb1[32];
+#pragma unroll
+      for (int c = 0; c < 2; ++c) {
+        float z1[16], dh[16];
+        tc::tmem_ld16(trow + 32 * h + 16 * c, z1);
+        tc::tmem_ld16(trow + 128 + 32 * h + 16 * c, dh);
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+          const int j = 32 * h + 16 * c + i;
+          const float dz = (z1[i] + sb1[j]) > 0.f ? dh[i] : 0.f;
+          gb1[16 * c + i] = dz;
+          st2(S::AT + tc::kmaj_off(kMlpH + j, tid, kTrainRows), __float2bfloat16(dz));
+        }
+      }
+      atomicAdd(G + kOffB1 + 32 * h + lane, tc::warp_column_sums32(gb1));
+    }
+    tc::fence_smem_to_async();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    // ---- [dW2 ; dW1] = [dZ2^T ; dZ1^T] [H1 | X] ----------------------------------------------------
+    ok = run([&] {
+      for (int kk = 0; kk < kTrainRows / 16; ++kk)
+        tc::mma_bf16(tmem + 0, tc::kmaj_desc(smem + S::AT, kTrainRows, kk), tc::kmaj_desc(smem + S::BT, kTrainRows, kk),
+                     id80, kk > 0);
+    });
   }
-  if (lane == 0) {
-    atomicAdd(G + kOffB3, db3);
-    atomicAdd(loss, lsum);
+  if (ok) {
+    if (w < 2) {  // rows 0-63: dW2 [n2 = tid][k1]
+#pragma unroll
+      for (int c = 0; c < kMlpH / 16; ++c) {
+        float g[16];
+        tc::tmem_ld16(trow + 16 * c, g);
+#pragma unroll
+        for (int i = 0; i < 16; ++i) atomicAdd(G + kOffW2 + tid * kMlpH + 16 * c + i, g[i]);
+      }
+    } else {  // rows 64-127: dW1 [n1 = tid - 64][k], columns 64-79
+      float g[16];
+      tc::tmem_ld16(trow + kMlpH, g);
+#pragma unroll
+      for (int k = 0; k < kMlpIn; ++k) atomicAdd(G + kOffW1 + (tid - kMlpH) * kMlpK1 + k, g[k]);
+    }
   }
+  tc::fence_before_sync();
   __syncthreads();
-  // dW2 [n2][k1] = dZ2^T H1 and dW1 [n1][k0] = dZ1^T X over the CTA's 64 samples; warp w owns
-  // output rows 16 w .. 16 w + 15
-#pragma unroll
-  for (int j = 0; j < 8; ++j) {
-    float c[4] = {0.f, 0.f, 0.f, 0.f};
-#pragma unroll
-    for (int kk = 0; kk < kTrainRows / 16; ++kk) {
-      unsigned a[4], b[2];
-      frag_a(a, dZ2T, kTrainRows, 16 * w, 16 * kk);
-      frag_bt(b, H1T, kTrainRows, 8 * j, 16 * kk);
-      mma_bf16(c, a, b);
-    }
-    float *gw = G + kOffW2 + (16 * w + g) * kMlpH + 8 * j + 2 * t;
-    atomicAdd(gw, c[0]);
-    atomicAdd(gw + 1, c[1]);
-    atomicAdd(gw + 8 * kMlpH, c[2]);
-    atomicAdd(gw + 8 * kMlpH + 1, c[3]);
-  }
-#pragma unroll
-  for (int j = 0; j < 2; ++j) {
-    float c[4] = {0.f, 0.f, 0.f, 0.f};
-#pragma unroll
-    for (int kk = 0; kk < kTrainRows / 16; ++kk) {
-      unsigned a[4], b[2];
-      frag_a(a, dZ1T, kTrainRows, 16 * w, 16 * kk);
-      frag_bt(b, XT, kTrainRows, 8 * j, 16 * kk);
-      mma_bf16(c, a, b);
-    }
-    const int k0 = 8 * j + 2 * t;
-    float *gw = G + kOffW1 + (16 * w + g) * kMlpK1 + k0;
-    if (k0 < kMlpIn) {
-      atomicAdd(gw, c[0]);
-      atomicAdd(gw + 8 * kMlpK1, c[2]);
-    }
-    if (k0 + 1 < kMlpIn) {
-      atomicAdd(gw + 1, c[1]);
-      atomicAdd(gw + 8 * kMlpK1 + 1, c[3]);
-    }
-  }
+  if (w == 0) tc::tmem_dealloc(tmem, kGradCols);
 }
 
-constexpr size_t kGradSmem = (size_t)(kMlpH * kMlpK1 + 2 * kMlpH * kMlpH + kMlpN3 * kMlpH + kMlpK1 * kTrainRows +
-                                      3 * kMlpH * kTrainRows) * 2 + 2 * kMlpH * 4;
+constexpr size_t kGradSmem = GradSmem::BYTES;
 
 // Replays logged solves from the plain guess or the learned one; ghost lanes past n re-solve the
 // last record so every warp is complete for the tensor-core guess, and write nothing.
@@ -513,7 +571,10 @@ int mlp_train(Context &c, const eqd_mlp_train_options &o, float *epoch_loss, flo
     nhold = (long long)(o.holdout * valid.size());
     ntrain = (long long)valid.size() - nhold;
     if ((rc = dmalloc(reinterpret_cast<void **>(&order), sizeof(int) * valid.size()))) break;
-    if ((rc = dmalloc(reinterpret_cast<void **>(&dloss), sizeof(float)))) break;
+    // dloss[0] the loss sum, dloss[1] (as int) the kernels' error word
+    if ((rc = dmalloc(reinterpret_cast<void **>(&dloss), 2 * sizeof(float)))) break;
+    cudaMemset(dloss, 0, 2 * sizeof(float));
+    int *derr = reinterpret_cast<int *>(dloss + 1);
     // parameters
     const std::vector<float> p0 = init_params(o.seed);
     cudaMemcpy(c.mlp_p, p0.data(), sizeof(float) * kMlpParams, cudaMemcpyHostToDevice);
@@ -535,7 +596,7 @@ int mlp_train(Context &c, const eqd_mlp_train_options &o, float *epoch_loss, flo
         TrainBatch tb{X, Y, order, b0, std::min<long long>(bs, ntrain - b0), 0.f};
         tb.inv_count = 1.f / (float)tb.count;
         const unsigned grid = (unsigned)((tb.count + kTrainRows - 1) / kTrainRows);
-        mlp_grad_kernel<<<grid, 128, kGradSmem>>>(static_cast<MlpDevice *>(c.mlp), tb, c.mlp_g, dloss);
+        mlp_grad_kernel<<<grid, kTrainRows, kGradSmem>>>(static_cast<MlpDevice *>(c.mlp), tb, c.mlp_g, dloss, derr);
         ++c.mlp_steps;
         const double t = (double)c.mlp_steps;
         const float lr_t = (float)(o.lr * std::sqrt(1.0 - std::pow(beta2, t)) / (1.0 - std::pow(beta1, t)));
@@ -556,13 +617,16 @@ int mlp_train(Context &c, const eqd_mlp_train_options &o, float *epoch_loss, flo
         cudaMemset(gscratch, 0, sizeof(float) * kMlpParams);
         cudaMemset(dloss, 0, sizeof(float));
         TrainBatch tb{X, Y, order, ntrain, nhold, 1.f / (float)nhold};
-        mlp_grad_kernel<<<(unsigned)((nhold + kTrainRows - 1) / kTrainRows), 128, kGradSmem>>>(
-            static_cast<MlpDevice *>(c.mlp), tb, gscratch, dloss);
+        mlp_grad_kernel<<<(unsigned)((nhold + kTrainRows - 1) / kTrainRows), kTrainRows, kGradSmem>>>(
+            static_cast<MlpDevice *>(c.mlp), tb, gscratch, dloss, derr);
         if (cudaMemcpy(holdout_loss, dloss, sizeof(float), cudaMemcpyDeviceToHost) != cudaSuccess) rc = EQD_ERR_CUDA;
         cudaFree(gscratch);
       }
     }
     if (cudaDeviceSynchronize() != cudaSuccess) rc = EQD_ERR_CUDA;
+    int herr = 0;
+    if (!rc && cudaMemcpy(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) rc = EQD_ERR_CUDA;
+    if (!rc && herr) rc = EQD_ERR_TIMEOUT;
   } while (false);
   if (raw) cudaFree(raw);
   if (X) cudaFree(X);
@@ -640,12 +704,12 @@ extern "C" int eqd_mlp_gradient(int32_t device, const float *params, const float
     G = P + kMlpParams;
     if ((rc = dmalloc(reinterpret_cast<void **>(&X), sizeof(__nv_bfloat16) * hx.size()))) break;
     if ((rc = dmalloc(reinterpret_cast<void **>(&Y), sizeof(float) * n))) break;
-    if ((rc = dmalloc(reinterpret_cast<void **>(&dl), sizeof(float)))) break;
+    if ((rc = dmalloc(reinterpret_cast<void **>(&dl), 2 * sizeof(float)))) break;  // loss, error word
     cudaMemcpy(P, params, sizeof(float) * kMlpParams, cudaMemcpyHostToDevice);
     cudaMemset(G, 0, sizeof(float) * kMlpParams);
     cudaMemcpy(X, hx.data(), sizeof(__nv_bfloat16) * hx.size(), cudaMemcpyHostToDevice);
     cudaMemcpy(Y, y, sizeof(float) * n, cudaMemcpyHostToDevice);
-    cudaMemset(dl, 0, sizeof(float));
+    cudaMemset(dl, 0, 2 * sizeof(float));
     mlp_sync_kernel<<<(kMlpParams + 255) / 256, 256>>>(P, m, nullptr);
     if (cudaFuncSetAttribute(mlp_grad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kGradSmem) !=
         cudaSuccess) {
@@ -653,11 +717,19 @@ extern "C" int eqd_mlp_gradient(int32_t device, const float *params, const float
       break;
     }
     TrainBatch tb{X, Y, nullptr, 0, n, 1.f / (float)n};
-    mlp_grad_kernel<<<(unsigned)((n + kTrainRows - 1) / kTrainRows), 128, kGradSmem>>>(m, tb, G, dl);
+    mlp_grad_kernel<<<(unsigned)((n + kTrainRows - 1) / kTrainRows), kTrainRows, kGradSmem>>>(
+        m, tb, G, dl, reinterpret_cast<int *>(dl + 1));
+    float h[2] = {0.f, 0.f};
     if (cudaDeviceSynchronize() != cudaSuccess ||
         cudaMemcpy(grad, G, sizeof(float) * kMlpParams, cudaMemcpyDeviceToHost) != cudaSuccess ||
-        cudaMemcpy(loss, dl, sizeof(float), cudaMemcpyDeviceToHost) != cudaSuccess)
+        cudaMemcpy(h, dl, sizeof(h), cudaMemcpyDeviceToHost) != cudaSuccess) {
       rc = EQD_ERR_CUDA;
+      break;
+    }
+    *loss = h[0];
+    int herr = 0;
+    std::memcpy(&herr, &h[1], sizeof(int));
+    if (herr) rc = EQD_ERR_TIMEOUT;
   } while (false);
   if (m) cudaFree(m);
   if (P) cudaFree(P);

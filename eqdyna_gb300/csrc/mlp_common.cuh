@@ -1,6 +1,8 @@
 // Learned initial guess for the rate-and-state Newton solve: a 6 -> 64 -> 64 -> 1 MLP (ReLU) in
-// BF16 weights and activations with FP32 accumulation, evaluated and trained on the tensor cores
-// with mma.sync.m16n8k16 (bf16 x bf16 -> f32).
+// BF16 weights and activations with FP32 accumulation.  This header holds the model block and the
+// inference fused into the fault kernel: each warp evaluates its 32 pairs with the warp-level
+// tensor-core MMA (mma.sync.m16n8k16, bf16 x bf16 -> f32), so no CTA-wide barrier or tensor memory
+// enters the per-pair solve.  Training runs on tcgen05 (kernels_mlp.cu).
 //
 // Inputs (raw features of one solve): ln V_trial (the slip rate the plain method starts from),
 // ln |state|, effective normal traction, trial shear traction, a, b.  Output: ln(V / V_trial) of the

@@ -251,7 +251,7 @@ int eqd_gpu_newton_counts(eqd_context *ctx, int64_t out[5]);
 
 typedef struct eqd_mlp_train_options {
   int32_t epochs;         /* passes over the training records                                  */
-  int32_t batch;          /* records per Adam step (rounded up to a multiple of 64)            */
+  int32_t batch;          /* records per Adam step (rounded up to a multiple of 128, >= 128)  */
   float lr;               /* Adam learning rate                                                */
   float holdout;          /* fraction of the records held out for the reported holdout loss    */
   uint64_t seed;          /* initial weights and shuffles                                      */
