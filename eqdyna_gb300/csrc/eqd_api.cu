@@ -34,7 +34,8 @@ struct eqd_context {
   Context c;
   double init_ms[8] = {};  // wall time of the setup phases (eqd_gpu_init_times)
   // host-side maps between the Fortran numbering and the device layout
-  std::vector<int> node_dev, node_orig;          // original node (0-based) <-> device id
+  std::vector<int> node_dev, node_orig;          // original node (0-based) <-> device id (-1: padding)
+  int nnode_mesh = 0;                            // nodes of the mesh (device nodes include padding)
   std::vector<int> gi_orig, gp_orig;             // device element slot -> original element
   std::vector<int> pair_station_col;             // on-fault station columns
   std::vector<double> times;                     // timeElapsed after n steps
@@ -43,6 +44,8 @@ struct eqd_context {
 };
 
 namespace {
+
+constexpr int kNodeBlock = 32;  // device node ranges are padded to multiples of this
 
 template <typename T>
 int dalloc(Context &c, T *&p, size_t n) {
@@ -572,7 +575,7 @@ int build_device_state(eqd_context &X, const eqd_scalars &s, const eqd_host_arra
   Context &c = X.c;
   c.sc = s;
   const int nn = a.nnode, ne = a.nelem;
-  c.nnode = nn;
+  X.nnode_mesh = nn;
   c.nelem = ne;
   c.neq = a.neq;
   c.nstep = s.nstep;
@@ -597,27 +600,57 @@ int build_device_state(eqd_context &X, const eqd_scalars &s, const eqd_host_arra
   auto eq_mass = [&](int node, int e) { return dev_tables ? dev_mass[node - 1] : a.nodalMassArr[e - 1]; };
   auto node_fnms = [&](int node) { return dev_tables ? dev_mass[node - 1] : a.fnms[node - 1]; };
   // ---- nodes ----
+  // Device order: the 3-DOF nodes, then the 12-DOF (PML) nodes, each range padded to whole blocks
+  // of kNodeBlock with inert nodes (1/m = 0, in no element, no force, state 0).  Every component
+  // of a node array (stride nnode) and of a PML array (stride npml) then starts on a 128-byte
+  // boundary and every warp of the node update reads and writes whole sectors: on C1 the update
+  // runs 5 % faster than with the mesh's counts.
+  // Within the ranges the node update tells its node classes by index: split (fault) nodes first
+  // among the 3-DOF nodes, PML nodes with equations before the fixed ones (src/driver.f90:141-144).
+  const int npair0 = (a.ntotft >= 1 && a.nftnd) ? a.nftnd[0] : 0;
+  std::vector<unsigned char> split_mesh(nn, 0);
+  for (int i = 0; i < npair0; ++i)
+    for (int k = 0; k < 2; ++k) {
+      const int node = a.nsmp[2 * (size_t)i + k];
+      if (node < 1 || node > nn) return EQD_ERR_INPUT;
+      split_mesh[node - 1] = 1;
+    }
   X.node_dev.assign(nn, -1);
   X.node_orig.clear();
+  auto place = [&](int j) { X.node_dev[j] = (int)X.node_orig.size(), X.node_orig.push_back(j); };
   for (int j = 0; j < nn; ++j)
-    if (a.numOfDofPerNodeArr[j] == 3) X.node_dev[j] = (int)X.node_orig.size(), X.node_orig.push_back(j);
+    if (a.numOfDofPerNodeArr[j] == 3 && split_mesh[j]) place(j);
+  c.n_split = (int)X.node_orig.size();
+  for (int j = 0; j < nn; ++j)
+    if (a.numOfDofPerNodeArr[j] == 3 && !split_mesh[j]) place(j);
+  while (X.node_orig.size() % kNodeBlock) X.node_orig.push_back(-1);
   c.n_int = (int)X.node_orig.size();
   for (int j = 0; j < nn; ++j) {
-    if (a.numOfDofPerNodeArr[j] == 12) X.node_dev[j] = (int)X.node_orig.size(), X.node_orig.push_back(j);
-    else if (a.numOfDofPerNodeArr[j] != 3) return EQD_ERR_INPUT;
+    if (a.numOfDofPerNodeArr[j] == 12 && eq(j + 1, 1) > 0) place(j);
+    else if (a.numOfDofPerNodeArr[j] != 3 && a.numOfDofPerNodeArr[j] != 12) return EQD_ERR_INPUT;
   }
-  c.npml = nn - c.n_int;
+  c.npml_live = (int)X.node_orig.size() - c.n_int;
+  for (int j = 0; j < nn; ++j)
+    if (a.numOfDofPerNodeArr[j] == 12 && !(eq(j + 1, 1) > 0)) place(j);
+  while (X.node_orig.size() % kNodeBlock) X.node_orig.push_back(-1);
+  const int nd = (int)X.node_orig.size();  // device nodes
+  c.nnode = nd;
+  c.npml = nd - c.n_int;
   const int np_ = c.npml;
-  Scratch<double> vel(3 * (size_t)nn), disp(3 * (size_t)nn);  // every entry written below
-  std::vector<double> F(3 * (size_t)nn, 0.0), inv_mass(nn, 0.0);
+  Scratch<double> vel(3 * (size_t)nd), disp(3 * (size_t)nd);  // every entry written below
+  std::vector<double> F(3 * (size_t)nd, 0.0), inv_mass(nd, 0.0);
   std::vector<double> F9(9 * (size_t)np_, 0.0), v9(9 * (size_t)np_, 0.0), vh(3 * (size_t)np_, 0.0);
   std::vector<double> pml_ab(6 * (size_t)np_, 0.0);
   int bad_ = EQD_OK;
 #pragma omp parallel for schedule(static)
-  for (int d = 0; d < nn; ++d) {
+  for (int d = 0; d < nd; ++d) {
     const int r_ = [&]() -> int {
       const int j = X.node_orig[d], node = j + 1;
-      for (int k = 0; k < 3; ++k) disp[k * (size_t)nn + d] = a.dispArr[3 * (size_t)j + k];
+      if (j < 0) {  // padding: zero state, 1/m = 0 (zero forces and PML factors above)
+        for (int k = 0; k < 3; ++k) disp[k * (size_t)nd + d] = 0.0, vel[k * (size_t)nd + d] = 0.0;
+        return EQD_OK;
+      }
+      for (int k = 0; k < 3; ++k) disp[k * (size_t)nd + d] = a.dispArr[3 * (size_t)j + k];
       if (d < c.n_int) {
         double m = -1;
         for (int k = 1; k <= 3; ++k) {
@@ -626,14 +659,14 @@ int build_device_state(eqd_context &X, const eqd_scalars &s, const eqd_host_arra
           const double mk = eq_mass(node, e);
           if (k == 1) m = mk;
           else if (mk != m) return EQD_ERR_UNSUPPORTED;  // anisotropic lumped mass: not built
-          vel[(k - 1) * (size_t)nn + d] = a.v1[e - 1];
-          F[(k - 1) * (size_t)nn + d] = a.nodalForceArr[e - 1];
+          vel[(k - 1) * (size_t)nd + d] = a.v1[e - 1];
+          F[(k - 1) * (size_t)nd + d] = a.nodalForceArr[e - 1];
         }
         if (!(m > 0)) return EQD_ERR_INPUT;
         inv_mass[d] = 1.0 / m;
       } else {
         const int p = d - c.n_int;
-        for (int k = 0; k < 3; ++k) vel[k * (size_t)nn + d] = a.velArr[3 * (size_t)j + k];
+        for (int k = 0; k < 3; ++k) vel[k * (size_t)nd + d] = a.velArr[3 * (size_t)j + k];
         const int e1 = eq(node, 1);
         if (e1 > 0) {
           const double m = eq_mass(node, e1);
@@ -647,7 +680,7 @@ int build_device_state(eqd_context &X, const eqd_scalars &s, const eqd_host_arra
               F9[(k - 1) * (size_t)np_ + p] = a.nodalForceArr[e - 1];
             } else {
               vh[(k - 10) * (size_t)np_ + p] = a.v1[e - 1];
-              F[(k - 10) * (size_t)nn + d] = a.nodalForceArr[e - 1];
+              F[(k - 10) * (size_t)nd + d] = a.nodalForceArr[e - 1];
             }
           }
           inv_mass[d] = 1.0 / m;
@@ -683,8 +716,7 @@ int build_device_state(eqd_context &X, const eqd_scalars &s, const eqd_host_arra
     // split (fault) nodes keep binary64 forces and updates: mark them with a negative 1/m and
     // give each a slot (2 i slave, 2 i + 1 master of pair i) in the binary64 force array
     std::vector<float> im32 = to_f32(inv_mass);
-    const int npair0 = (a.ntotft >= 1 && a.nftnd) ? a.nftnd[0] : 0;
-    std::vector<int> slot(nn, -1);
+    std::vector<int> slot(nd, -1);
     std::vector<double> fsplit(3 * (size_t)std::max(2 * npair0, 1), 0.0);
     for (int i = 0; i < npair0; ++i)
       for (int k = 0; k < 2; ++k) {
@@ -694,9 +726,9 @@ int build_device_state(eqd_context &X, const eqd_scalars &s, const eqd_host_arra
         if (d >= c.n_int) return EQD_ERR_UNSUPPORTED;
         slot[d] = 2 * i + k;
         im32[d] = -im32[d];
-        if (X.split_node.empty()) X.split_node.assign(nn, 0);
+        if (X.split_node.empty()) X.split_node.assign(nd, 0);
         X.split_node[d] = 1;
-        for (int q = 0; q < 3; ++q) fsplit[(size_t)q * 2 * npair0 + 2 * i + k] = F[(size_t)q * nn + d];
+        for (int q = 0; q < 3; ++q) fsplit[(size_t)q * 2 * npair0 + 2 * i + k] = F[(size_t)q * nd + d];
       }
     RC(dupload(c, c.inv_mass32, im32));
     RC(dupload(c, c.split_slot, slot));
@@ -1019,10 +1051,10 @@ int build_device_state(eqd_context &X, const eqd_scalars &s, const eqd_host_arra
     if (!qc.empty()) RC(dupload(c, g.qcoef, qc));
   }
   if (c.fp32) {
-    RC(dalloc(c, c.vel32, 3 * (size_t)nn));
-    RC(dalloc(c, c.dl32, 3 * (size_t)nn));
-    EQD_CUDA_OK(cudaMemset(c.vel32, 0, 3 * (size_t)nn * sizeof(float)));
-    EQD_CUDA_OK(cudaMemset(c.dl32, 0, 3 * (size_t)nn * sizeof(float)));
+    RC(dalloc(c, c.vel32, 3 * (size_t)nd));
+    RC(dalloc(c, c.dl32, 3 * (size_t)nd));
+    EQD_CUDA_OK(cudaMemset(c.vel32, 0, 3 * (size_t)nd * sizeof(float)));
+    EQD_CUDA_OK(cudaMemset(c.dl32, 0, 3 * (size_t)nd * sizeof(float)));
   }
 
   mark(4);
@@ -1634,7 +1666,7 @@ int eqd_gpu_fetch(eqd_context *X, eqd_host_arrays *a) {
   Context &c = X->c;
   cudaSetDevice(c.device);
   EQD_CUDA_OK(cudaStreamSynchronize(c.stream));
-  if (a->nnode != c.nnode || a->nelem != c.nelem) return EQD_ERR_INPUT;
+  if (a->nnode != X->nnode_mesh || a->nelem != c.nelem) return EQD_ERR_INPUT;
   const int nn = c.nnode, np_ = c.npml;
   Scratch<double> vel(3 * (size_t)nn), disp(3 * (size_t)nn), F(3 * (size_t)nn), im(nn);  // copied into
   std::vector<double> v9(9 * (size_t)np_), vh(3 * (size_t)np_), F9(9 * (size_t)np_);
@@ -1681,6 +1713,7 @@ int eqd_gpu_fetch(eqd_context *X, eqd_host_arrays *a) {
 #pragma omp parallel for schedule(static)
   for (int d = 0; d < nn; ++d) {
     const int j = X->node_orig[d];
+    if (j < 0) continue;  // padding
     for (int k = 0; k < 3; ++k) {
       if (a->velArr) a->velArr[3 * (size_t)j + k] = vel[k * (size_t)nn + d];
       if (a->dispArr) a->dispArr[3 * (size_t)j + k] = disp[k * (size_t)nn + d];

@@ -83,6 +83,9 @@ struct PairStation {
 struct Context {
   // sizes
   int nnode = 0, n_int = 0, npml = 0, nelem = 0, neq = 0;
+  // device node order: split (fault) nodes [0, n_split), the other 3-DOF nodes, padding up to
+  // n_int; PML nodes with equations [n_int, n_int + npml_live), fixed PML nodes, padding
+  int n_split = 0, npml_live = 0;
   int npair = 0, nstep = 0, nOnSt = 0, nOffRows = 0;
   int64_t size_stress = 0;
   eqd_scalars sc{};

@@ -96,6 +96,7 @@ struct NodeArgs32 {
   double *vh;
   const float *pml_ab;
   int nnode, n_int, npml, nsplit;
+  int n_split, npml_live;  // device order: split nodes first, fixed PML nodes after the live ones
   float dt;
   double dtd, rdampk;
   int *d_nt, *d_err;
@@ -158,12 +159,14 @@ __device__ __forceinline__ void node_update32_body(const NodeArgs32 &a, int i) {
   const int *__restrict__ split_slot = a.split_slot;
   if (i == 0) *a.d_nt += 1;
   if (i >= nnode) return;
-  const float im = inv_mass[i];
-  double v[3];
-  if (im < 0.f) {
+  // the node classes are index ranges (device order), so no test waits for a loaded value
+  if (i < a.n_split) {
     if (!a.skip_split) split_node_update<F_IS_ACC>(a, i, split_slot[i]);
     return;
-  } else if (i < n_int) {
+  }
+  const float im = inv_mass[i];
+  double v[3];
+  if (i < n_int) {
     float v32[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
@@ -184,7 +187,7 @@ __device__ __forceinline__ void node_update32_body(const NodeArgs32 &a, int i) {
     return;
   } else {
     const int p = i - n_int;
-    if (im == 0.f) {
+    if (p >= a.npml_live) {  // fixed PML node (or padding): 1/m = 0
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
         v[c] = 0.0;
@@ -657,6 +660,8 @@ NodeArgs32 node_args32(const Context &c) {
   a.nnode = c.nnode;
   a.n_int = c.n_int;
   a.npml = c.npml;
+  a.n_split = c.n_split;
+  a.npml_live = c.npml_live;
   a.dt = (float)c.sc.dt;
   a.dtd = c.sc.dt;
   a.d_nt = c.d_nt;
