@@ -615,24 +615,30 @@ int build_device_state(eqd_context &X, const eqd_scalars &s, const eqd_host_arra
       if (node < 1 || node > nn) return EQD_ERR_INPUT;
       split_mesh[node - 1] = 1;
     }
-  X.node_dev.assign(nn, -1);
-  X.node_orig.clear();
-  auto place = [&](int j) { X.node_dev[j] = (int)X.node_orig.size(), X.node_orig.push_back(j); };
-  for (int j = 0; j < nn; ++j)
-    if (a.numOfDofPerNodeArr[j] == 3 && split_mesh[j]) place(j);
-  c.n_split = (int)X.node_orig.size();
-  for (int j = 0; j < nn; ++j)
-    if (a.numOfDofPerNodeArr[j] == 3 && !split_mesh[j]) place(j);
-  while (X.node_orig.size() % kNodeBlock) X.node_orig.push_back(-1);
-  c.n_int = (int)X.node_orig.size();
+  std::vector<int> cls[4];  // split 3-DOF, other 3-DOF, PML with equations, fixed PML
   for (int j = 0; j < nn; ++j) {
-    if (a.numOfDofPerNodeArr[j] == 12 && eq(j + 1, 1) > 0) place(j);
-    else if (a.numOfDofPerNodeArr[j] != 3 && a.numOfDofPerNodeArr[j] != 12) return EQD_ERR_INPUT;
+    const int dof = a.numOfDofPerNodeArr[j];
+    if (dof == 3) cls[split_mesh[j] ? 0 : 1].push_back(j);
+    else if (dof == 12) cls[eq(j + 1, 1) > 0 ? 2 : 3].push_back(j);
+    else return EQD_ERR_INPUT;
   }
+  X.node_orig.clear();
+  X.node_orig.reserve((size_t)nn + 2 * kNodeBlock);
+  auto take = [&](const std::vector<int> &v) { X.node_orig.insert(X.node_orig.end(), v.begin(), v.end()); };
+  auto pad = [&]() { while (X.node_orig.size() % kNodeBlock) X.node_orig.push_back(-1); };
+  take(cls[0]);
+  c.n_split = (int)X.node_orig.size();
+  take(cls[1]);
+  pad();
+  c.n_int = (int)X.node_orig.size();
+  take(cls[2]);
   c.npml_live = (int)X.node_orig.size() - c.n_int;
-  for (int j = 0; j < nn; ++j)
-    if (a.numOfDofPerNodeArr[j] == 12 && !(eq(j + 1, 1) > 0)) place(j);
-  while (X.node_orig.size() % kNodeBlock) X.node_orig.push_back(-1);
+  take(cls[3]);
+  pad();
+  X.node_dev.assign(nn, -1);
+#pragma omp parallel for schedule(static)
+  for (int d = 0; d < (int)X.node_orig.size(); ++d)
+    if (X.node_orig[d] >= 0) X.node_dev[X.node_orig[d]] = d;
   const int nd = (int)X.node_orig.size();  // device nodes
   c.nnode = nd;
   c.npml = nd - c.n_int;
