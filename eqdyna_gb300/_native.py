@@ -222,6 +222,9 @@ def gpu_lib():
         lib.eqd_host_element_order.argtypes = [C.POINTER(EqdHostArrays), C.c_int32, C.c_int32,
                                                C.POINTER(C.c_int32), C.c_int64, i64_p, d_p]
         lib.eqd_host_element_order.restype = C.c_int
+        lib.eqd_host_node_order.argtypes = [C.POINTER(EqdHostArrays), C.POINTER(C.c_int32), C.c_int64, i64_p,
+                                            C.POINTER(C.c_int32)]
+        lib.eqd_host_node_order.restype = C.c_int
         _gpu_lib = lib
     return _gpu_lib
 
@@ -231,6 +234,7 @@ GPU_SYMBOLS = ["eqd_gpu_init", "eqd_gpu_step", "eqd_gpu_fetch", "eqd_gpu_fetch_f
                "eqd_gpu_finalize", "eqd_gpu_status_string", "eqd_gpu_stats", "eqd_gpu_time",
                "eqd_gpu_profile", "eqd_gpu_kernel_time", "eqd_gpu_newton_counts", "eqd_gpu_table_info",
                "eqd_gpu_fetch_fric_rows", "eqd_host_alloc", "eqd_host_free", "eqd_host_element_order",
+               "eqd_host_node_order",
                "eqd_gpu_step_async",
                "eqd_gpu_fetch_fric_rows_async", "eqd_gpu_fetch_wait", "eqd_gpu_output_setup",
                "eqd_gpu_output_drain",

@@ -565,6 +565,58 @@ int group_tables_from_device(const DeviceMesh &dm, const std::vector<int> &ids, 
   return rc;
 }
 
+// Device node order: the 3-DOF nodes, then the 12-DOF (PML) nodes, each range padded to whole
+// blocks of kNodeBlock with inert nodes (1/m = 0, in no element, no force, state 0).  Every
+// component of a node array (stride nnode) and of a PML array (stride npml) then starts on a
+// 128-byte boundary and every warp of the node update reads and writes whole sectors: on C1 the
+// update runs 5 % faster than with the mesh's counts.  Within the ranges the node update tells its
+// node classes by index: split (fault) nodes of the first fault first among the 3-DOF nodes, PML
+// nodes with equations before the fixed ones (src/driver.f90:141-144).  Within a class the mesh
+// order is kept.
+struct NodeOrder {
+  std::vector<int> orig;  // device node -> 0-based mesh node, -1 for padding
+  int n_split = 0, n_int = 0, npml_live = 0;
+};
+int device_node_order(const eqd_host_arrays &a, NodeOrder &o) {
+  const int nn = a.nnode;
+  if (nn <= 0 || !a.numOfDofPerNodeArr || !a.eqNumStartIndexLoc || !a.eqNumIndexArr) return EQD_ERR_INPUT;
+  auto eq1 = [&](int j) -> int {  // 0-based node -> 1-based equation of its first DOF, or <= 0
+    const int loc = a.eqNumStartIndexLoc[j] + 1;
+    if (loc < 1 || loc > a.size_eqidx) return -2;
+    return a.eqNumIndexArr[loc - 1];
+  };
+  const int npair0 = (a.ntotft >= 1 && a.nftnd) ? a.nftnd[0] : 0;
+  if (npair0 > 0 && !a.nsmp) return EQD_ERR_INPUT;
+  std::vector<unsigned char> split_mesh(nn, 0);
+  for (int i = 0; i < npair0; ++i)
+    for (int k = 0; k < 2; ++k) {
+      const int node = a.nsmp[2 * (size_t)i + k];
+      if (node < 1 || node > nn) return EQD_ERR_INPUT;
+      split_mesh[node - 1] = 1;
+    }
+  std::vector<int> cls[4];  // split 3-DOF, other 3-DOF, PML with equations, fixed PML
+  for (int j = 0; j < nn; ++j) {
+    const int dof = a.numOfDofPerNodeArr[j];
+    if (dof == 3) cls[split_mesh[j] ? 0 : 1].push_back(j);
+    else if (dof == 12) cls[eq1(j) > 0 ? 2 : 3].push_back(j);
+    else return EQD_ERR_INPUT;
+  }
+  o.orig.clear();
+  o.orig.reserve((size_t)nn + 2 * kNodeBlock);
+  auto take = [&](const std::vector<int> &v) { o.orig.insert(o.orig.end(), v.begin(), v.end()); };
+  auto pad = [&]() { while (o.orig.size() % kNodeBlock) o.orig.push_back(-1); };
+  take(cls[0]);
+  o.n_split = (int)o.orig.size();
+  take(cls[1]);
+  pad();
+  o.n_int = (int)o.orig.size();
+  take(cls[2]);
+  o.npml_live = (int)o.orig.size() - o.n_int;
+  take(cls[3]);
+  pad();
+  return EQD_OK;
+}
+
 int build_device_state(eqd_context &X, const eqd_scalars &s, const eqd_host_arrays &a) {
   auto t_last = std::chrono::steady_clock::now();
   auto mark = [&](int k) {
@@ -600,41 +652,14 @@ int build_device_state(eqd_context &X, const eqd_scalars &s, const eqd_host_arra
   auto eq_mass = [&](int node, int e) { return dev_tables ? dev_mass[node - 1] : a.nodalMassArr[e - 1]; };
   auto node_fnms = [&](int node) { return dev_tables ? dev_mass[node - 1] : a.fnms[node - 1]; };
   // ---- nodes ----
-  // Device order: the 3-DOF nodes, then the 12-DOF (PML) nodes, each range padded to whole blocks
-  // of kNodeBlock with inert nodes (1/m = 0, in no element, no force, state 0).  Every component
-  // of a node array (stride nnode) and of a PML array (stride npml) then starts on a 128-byte
-  // boundary and every warp of the node update reads and writes whole sectors: on C1 the update
-  // runs 5 % faster than with the mesh's counts.
-  // Within the ranges the node update tells its node classes by index: split (fault) nodes first
-  // among the 3-DOF nodes, PML nodes with equations before the fixed ones (src/driver.f90:141-144).
-  const int npair0 = (a.ntotft >= 1 && a.nftnd) ? a.nftnd[0] : 0;
-  std::vector<unsigned char> split_mesh(nn, 0);
-  for (int i = 0; i < npair0; ++i)
-    for (int k = 0; k < 2; ++k) {
-      const int node = a.nsmp[2 * (size_t)i + k];
-      if (node < 1 || node > nn) return EQD_ERR_INPUT;
-      split_mesh[node - 1] = 1;
-    }
-  std::vector<int> cls[4];  // split 3-DOF, other 3-DOF, PML with equations, fixed PML
-  for (int j = 0; j < nn; ++j) {
-    const int dof = a.numOfDofPerNodeArr[j];
-    if (dof == 3) cls[split_mesh[j] ? 0 : 1].push_back(j);
-    else if (dof == 12) cls[eq(j + 1, 1) > 0 ? 2 : 3].push_back(j);
-    else return EQD_ERR_INPUT;
+  {
+    NodeOrder o;
+    RC(device_node_order(a, o));
+    X.node_orig.swap(o.orig);
+    c.n_split = o.n_split;
+    c.n_int = o.n_int;
+    c.npml_live = o.npml_live;
   }
-  X.node_orig.clear();
-  X.node_orig.reserve((size_t)nn + 2 * kNodeBlock);
-  auto take = [&](const std::vector<int> &v) { X.node_orig.insert(X.node_orig.end(), v.begin(), v.end()); };
-  auto pad = [&]() { while (X.node_orig.size() % kNodeBlock) X.node_orig.push_back(-1); };
-  take(cls[0]);
-  c.n_split = (int)X.node_orig.size();
-  take(cls[1]);
-  pad();
-  c.n_int = (int)X.node_orig.size();
-  take(cls[2]);
-  c.npml_live = (int)X.node_orig.size() - c.n_int;
-  take(cls[3]);
-  pad();
   X.node_dev.assign(nn, -1);
 #pragma omp parallel for schedule(static)
   for (int d = 0; d < (int)X.node_orig.size(); ++d)
@@ -722,6 +747,7 @@ int build_device_state(eqd_context &X, const eqd_scalars &s, const eqd_host_arra
     // split (fault) nodes keep binary64 forces and updates: mark them with a negative 1/m and
     // give each a slot (2 i slave, 2 i + 1 master of pair i) in the binary64 force array
     std::vector<float> im32 = to_f32(inv_mass);
+    const int npair0 = (a.ntotft >= 1 && a.nftnd) ? a.nftnd[0] : 0;
     std::vector<int> slot(nd, -1);
     std::vector<double> fsplit(3 * (size_t)std::max(2 * npair0, 1), 0.0);
     for (int i = 0; i < npair0; ++i)
@@ -2218,6 +2244,21 @@ int eqd_host_element_order(const eqd_host_arrays *a, int32_t group, int32_t tile
   *n_out = (int64_t)ids.size();
   if (!out || cap < (int64_t)ids.size()) return out ? EQD_ERR_INPUT : EQD_OK;
   std::copy(ids.begin(), ids.end(), out);
+  return EQD_OK;
+}
+
+int eqd_host_node_order(const eqd_host_arrays *a, int32_t *out, int64_t cap, int64_t *n_out, int32_t counts[4]) {
+  if (!a || !n_out || !counts) return EQD_ERR_INPUT;
+  NodeOrder o;
+  const int rc = device_node_order(*a, o);
+  if (rc) return rc;
+  counts[0] = o.n_split;
+  counts[1] = o.n_int;
+  counts[2] = o.npml_live;
+  counts[3] = (int32_t)o.orig.size();
+  *n_out = (int64_t)o.orig.size();
+  if (!out || cap < (int64_t)o.orig.size()) return out ? EQD_ERR_INPUT : EQD_OK;
+  std::copy(o.orig.begin(), o.orig.end(), out);
   return EQD_OK;
 }
 

@@ -343,6 +343,15 @@ int eqd_gpu_table_info(eqd_context *ctx, int32_t group, int64_t info[8]);
 int eqd_host_element_order(const eqd_host_arrays *a, int32_t group, int32_t tile_shape, int32_t *out,
                            int64_t cap, int64_t *n_out, double *live);
 
+/* Host only (no GPU needed): the device node order eqd_gpu_init uses.  out[0 .. *n_out) = the
+ * 0-based mesh node of each device node, -1 for a padding node; counts = {split (fault) nodes,
+ * first device node of the PML range (the 3-DOF range padded to a multiple of 32), PML nodes with
+ * equations, device nodes (a multiple of 32)}.  Device order: split nodes of the first fault, the
+ * other 3-DOF nodes, padding, PML nodes with equations, fixed PML nodes, padding; mesh order within
+ * each class.  With out == NULL only *n_out and counts are set; a cap below *n_out returns
+ * EQD_ERR_INPUT. */
+int eqd_host_node_order(const eqd_host_arrays *a, int32_t *out, int64_t cap, int64_t *n_out, int32_t counts[4]);
+
 /* Setup on the GPU: the per-element tables and lumped nodal masses that the reference builds on
  * the host before its time loop (assembleGlobalMass, src/assembleGlobalMass.f90:12-38,283-406;
  * calcGlobalShapeFunc, src/calcGlobalShapeFunc.f90:1-75; calcSSPhi4Hrgls,
