@@ -424,8 +424,9 @@ int build_tiles(Context &c, ElemGroup<float> &g, const Scratch<int> &conn_dev, i
   return EQD_OK;
 }
 
-std::vector<float> to_f32(const std::vector<double> &v) {
-  std::vector<float> out(v.size());
+template <class A>
+Scratch<float> to_f32(const std::vector<double, A> &v) {
+  Scratch<float> out(v.size());
 #pragma omp parallel for schedule(static)
   for (long long i = 0; i < (long long)v.size(); ++i) out[i] = (float)v[i];
   return out;
@@ -594,26 +595,30 @@ int device_node_order(const eqd_host_arrays &a, NodeOrder &o) {
       if (node < 1 || node > nn) return EQD_ERR_INPUT;
       split_mesh[node - 1] = 1;
     }
-  std::vector<int> cls[4];  // split 3-DOF, other 3-DOF, PML with equations, fixed PML
+  // class of each node (0 split 3-DOF, 1 other 3-DOF, 2 PML with equations, 3 fixed PML), then a
+  // stable counting scatter into the device order
+  Scratch<unsigned char> klass(nn);
+  long long count[4] = {0, 0, 0, 0};
+  int bad = 0;
+#pragma omp parallel for schedule(static) reduction(+ : count[:4]) reduction(| : bad)
   for (int j = 0; j < nn; ++j) {
     const int dof = a.numOfDofPerNodeArr[j];
-    if (dof == 3) cls[split_mesh[j] ? 0 : 1].push_back(j);
-    else if (dof == 12) cls[eq1(j) > 0 ? 2 : 3].push_back(j);
-    else return EQD_ERR_INPUT;
+    unsigned char k = 0;
+    if (dof == 3) k = split_mesh[j] ? 0 : 1;
+    else if (dof == 12) k = eq1(j) > 0 ? 2 : 3;
+    else bad = 1;
+    klass[j] = k;
+    ++count[k];
   }
-  o.orig.clear();
-  o.orig.reserve((size_t)nn + 2 * kNodeBlock);
-  auto take = [&](const std::vector<int> &v) { o.orig.insert(o.orig.end(), v.begin(), v.end()); };
-  auto pad = [&]() { while (o.orig.size() % kNodeBlock) o.orig.push_back(-1); };
-  take(cls[0]);
-  o.n_split = (int)o.orig.size();
-  take(cls[1]);
-  pad();
-  o.n_int = (int)o.orig.size();
-  take(cls[2]);
-  o.npml_live = (int)o.orig.size() - o.n_int;
-  take(cls[3]);
-  pad();
+  if (bad) return EQD_ERR_INPUT;
+  auto up = [](long long x) { return (x + kNodeBlock - 1) / kNodeBlock * kNodeBlock; };
+  o.n_split = (int)count[0];
+  o.n_int = (int)up(count[0] + count[1]);
+  o.npml_live = (int)count[2];
+  const long long total = o.n_int + up(count[2] + count[3]);
+  long long cursor[4] = {0, count[0], o.n_int, o.n_int + count[2]};
+  o.orig.assign((size_t)total, -1);
+  for (int j = 0; j < nn; ++j) o.orig[(size_t)cursor[klass[j]]++] = j;
   return EQD_OK;
 }
 
@@ -669,9 +674,16 @@ int build_device_state(eqd_context &X, const eqd_scalars &s, const eqd_host_arra
   c.npml = nd - c.n_int;
   const int np_ = c.npml;
   Scratch<double> vel(3 * (size_t)nd), disp(3 * (size_t)nd);  // every entry written below
-  std::vector<double> F(3 * (size_t)nd, 0.0), inv_mass(nd, 0.0);
-  std::vector<double> F9(9 * (size_t)np_, 0.0), v9(9 * (size_t)np_, 0.0), vh(3 * (size_t)np_, 0.0);
-  std::vector<double> pml_ab(6 * (size_t)np_, 0.0);
+  // zeroed by all host threads (a value-initialised vector is filled by one)
+  auto zeros = [](size_t n) {
+    Scratch<double> v(n);
+#pragma omp parallel for schedule(static)
+    for (long long i = 0; i < (long long)n; ++i) v[i] = 0.0;
+    return v;
+  };
+  Scratch<double> F = zeros(3 * (size_t)nd), inv_mass = zeros(nd);
+  Scratch<double> F9 = zeros(9 * (size_t)np_), v9 = zeros(9 * (size_t)np_), vh = zeros(3 * (size_t)np_);
+  Scratch<double> pml_ab = zeros(6 * (size_t)np_);
   int bad_ = EQD_OK;
 #pragma omp parallel for schedule(static)
   for (int d = 0; d < nd; ++d) {
@@ -746,7 +758,7 @@ int build_device_state(eqd_context &X, const eqd_scalars &s, const eqd_host_arra
     RC(dupload(c, c.pml_ab32, to_f32(pml_ab)));
     // split (fault) nodes keep binary64 forces and updates: mark them with a negative 1/m and
     // give each a slot (2 i slave, 2 i + 1 master of pair i) in the binary64 force array
-    std::vector<float> im32 = to_f32(inv_mass);
+    Scratch<float> im32 = to_f32(inv_mass);
     const int npair0 = (a.ntotft >= 1 && a.nftnd) ? a.nftnd[0] : 0;
     std::vector<int> slot(nd, -1);
     std::vector<double> fsplit(3 * (size_t)std::max(2 * npair0, 1), 0.0);
