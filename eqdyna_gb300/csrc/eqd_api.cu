@@ -82,6 +82,13 @@ struct NoInitAlloc : std::allocator<T> {
 };
 template <class T>
 using Scratch = std::vector<T, NoInitAlloc<T>>;
+// n zeros written by all host threads (a value-initialised vector is filled by one)
+Scratch<double> zeros64(size_t n) {
+  Scratch<double> v(n);
+#pragma omp parallel for schedule(static)
+  for (long long i = 0; i < (long long)n; ++i) v[i] = 0.0;
+  return v;
+}
 
 template <typename T, class A>
 int dupload(Context &c, T *&p, const std::vector<T, A> &h) {
@@ -492,13 +499,13 @@ inline long auto_max_records(int record_floats) { return kAutoRecordBytes / (4l 
 
 // binary32 copy of a component-major table [ncomp][m] with its rows padded with zeros to stride ld
 template <class V>
-std::vector<float> to_f32_rows(const V &v, size_t m, size_t ld) {
+Scratch<float> to_f32_rows(const V &v, size_t m, size_t ld) {
   const size_t nc = v.size() / m;
-  std::vector<float> out(nc * ld, 0.f);
+  Scratch<float> out(nc * ld);
 #pragma omp parallel for schedule(static)
-  for (long long qi = 0; qi < (long long)(nc * m); ++qi) {
-    const size_t q = (size_t)qi / m, i = (size_t)qi % m;
-    out[q * ld + i] = (float)v[qi];
+  for (long long qi = 0; qi < (long long)(nc * ld); ++qi) {
+    const size_t q = (size_t)qi / ld, i = (size_t)qi % ld;
+    out[qi] = i < m ? (float)v[q * m + i] : 0.f;  // rows padded to ld with zeros
   }
   return out;
 }
@@ -528,7 +535,7 @@ int validate(const eqd_scalars *s, const eqd_host_arrays *a) {
 // and copied into the group's host rows (shp[q * m + i] ...), in chunks of device scratch.
 template <class V>
 int group_tables_from_device(const DeviceMesh &dm, const std::vector<int> &ids, int m, double w, V &shp, V &phi,
-                             V &ss, V &detw, std::vector<double> *em) {
+                             V &ss, V &detw, V *em) {
   if (m <= 0) return EQD_OK;
   const int cn = std::min(m, 1 << 22);
   double *d = nullptr;
@@ -674,16 +681,9 @@ int build_device_state(eqd_context &X, const eqd_scalars &s, const eqd_host_arra
   c.npml = nd - c.n_int;
   const int np_ = c.npml;
   Scratch<double> vel(3 * (size_t)nd), disp(3 * (size_t)nd);  // every entry written below
-  // zeroed by all host threads (a value-initialised vector is filled by one)
-  auto zeros = [](size_t n) {
-    Scratch<double> v(n);
-#pragma omp parallel for schedule(static)
-    for (long long i = 0; i < (long long)n; ++i) v[i] = 0.0;
-    return v;
-  };
-  Scratch<double> F = zeros(3 * (size_t)nd), inv_mass = zeros(nd);
-  Scratch<double> F9 = zeros(9 * (size_t)np_), v9 = zeros(9 * (size_t)np_), vh = zeros(3 * (size_t)np_);
-  Scratch<double> pml_ab = zeros(6 * (size_t)np_);
+  Scratch<double> F = zeros64(3 * (size_t)nd), inv_mass = zeros64(nd);
+  Scratch<double> F9 = zeros64(9 * (size_t)np_), v9 = zeros64(9 * (size_t)np_), vh = zeros64(3 * (size_t)np_);
+  Scratch<double> pml_ab = zeros64(6 * (size_t)np_);
   int bad_ = EQD_OK;
 #pragma omp parallel for schedule(static)
   for (int d = 0; d < nd; ++d) {
@@ -818,14 +818,14 @@ int build_device_state(eqd_context &X, const eqd_scalars &s, const eqd_host_arra
     Scratch<double> shp(24 * (size_t)m), phi(32 * (size_t)m), ss(6 * (size_t)m), detw(m), lam(m), mu(m);
     const int nstress = grp == 0 ? (s.C_Q != 0 ? 12 : 6) : 15;
     Scratch<double> st(nstress * (size_t)m);
-    std::vector<double> st0, pab, em, hg, porep, pstr, qc;
+    Scratch<double> st0, pab, em, hg, porep, pstr, qc;
     bool any_s0 = false;
     int s0_any = 0;
-    if (grp == 1) st0.assign(6 * (size_t)m, 0.0), pab.assign(6 * (size_t)m, 0.0);
-    if (body) em.assign(8 * (size_t)m, 0.0);
-    if (s.C_hg == 2) hg.assign(m, 0.0);
-    if (grp == 0 && s.C_elastic == 0) porep.assign(m, 0.0), pstr.assign(m, 0.0);
-    if (grp == 0 && s.C_Q != 0) qc.assign(5 * (size_t)m, 0.0);
+    if (grp == 1) st0 = zeros64(6 * (size_t)m), pab = zeros64(6 * (size_t)m);
+    if (body) em = zeros64(8 * (size_t)m);
+    if (s.C_hg == 2) hg = zeros64(m);
+    if (grp == 0 && s.C_elastic == 0) porep = zeros64(m), pstr = zeros64(m);
+    if (grp == 0 && s.C_Q != 0) qc = zeros64(5 * (size_t)m);
     int bad_ = EQD_OK;
 #pragma omp parallel for schedule(static) reduction(|| : s0_any)
     for (int i = 0; i < m; ++i) {
@@ -1713,12 +1713,12 @@ int eqd_gpu_fetch(eqd_context *X, eqd_host_arrays *a) {
   if (a->nnode != X->nnode_mesh || a->nelem != c.nelem) return EQD_ERR_INPUT;
   const int nn = c.nnode, np_ = c.npml;
   Scratch<double> vel(3 * (size_t)nn), disp(3 * (size_t)nn), F(3 * (size_t)nn), im(nn);  // copied into
-  std::vector<double> v9(9 * (size_t)np_), vh(3 * (size_t)np_), F9(9 * (size_t)np_);
+  Scratch<double> v9(9 * (size_t)np_), vh(3 * (size_t)np_), F9(9 * (size_t)np_);  // (no serial zero fill)
   EQD_CUDA_OK(cudaMemcpy(vel.data(), c.vel, vel.size() * 8, cudaMemcpyDeviceToHost));
   EQD_CUDA_OK(cudaMemcpy(disp.data(), c.disp, disp.size() * 8, cudaMemcpyDeviceToHost));
   EQD_CUDA_OK(cudaMemcpy(im.data(), c.inv_mass, im.size() * 8, cudaMemcpyDeviceToHost));
   auto get32 = [&](auto &dst, const float *src) -> int {
-    std::vector<float> t(dst.size());
+    Scratch<float> t(dst.size());
     if (!t.empty() && cudaMemcpy(t.data(), src, t.size() * 4, cudaMemcpyDeviceToHost) != cudaSuccess) return EQD_ERR_CUDA;
     const long long nt = (long long)t.size();
 #pragma omp parallel for schedule(static)
@@ -1787,30 +1787,32 @@ int eqd_gpu_fetch(eqd_context *X, eqd_host_arrays *a) {
       const int m = (int)ids.size();
       if (m == 0) continue;
       const int nstress = grp == 0 ? (c.sc.C_Q != 0 ? 12 : 6) : 15;
-      std::vector<double> st(nstress * (size_t)m);
+      // stress component q of device slot i at src[q * ld + i], into the element's stressArr entries
+      auto scatter = [&](const auto *src, size_t ld) {
+#pragma omp parallel for schedule(static)
+        for (int i = 0; i < m; ++i) {
+          if (ids[i] < 0) continue;  // empty slot of the binary32 tiles
+          const int64_t base = a->stressCompIndexArr[ids[i]];
+          for (int q = 0; q < nstress; ++q) a->stressArr[base + q] = (double)src[q * ld + i];
+        }
+      };
       if (c.fp32) {
         const ElemGroup<float> &g = grp == 0 ? c.gi32 : c.gp32;
-        std::vector<float> s32(nstress * (size_t)g.ld);
+        Scratch<float> s32(nstress * (size_t)g.ld);
         EQD_CUDA_OK(cudaMemcpy(s32.data(), g.stress, s32.size() * 4, cudaMemcpyDeviceToHost));
-#pragma omp parallel for schedule(static)
-        for (int i = 0; i < m; ++i)
-          for (int q = 0; q < nstress; ++q) st[q * (size_t)m + i] = s32[q * (size_t)g.ld + i];
+        scatter(s32.data(), (size_t)g.ld);
       } else {
         const ElemGroup<double> &g = grp == 0 ? c.gi64 : c.gp64;
+        Scratch<double> st(nstress * (size_t)m);
         EQD_CUDA_OK(cudaMemcpy(st.data(), g.stress, st.size() * 8, cudaMemcpyDeviceToHost));
-      }
-#pragma omp parallel for schedule(static)
-      for (int i = 0; i < m; ++i) {
-        if (ids[i] < 0) continue;  // empty slot of the binary32 tiles
-        const int64_t base = a->stressCompIndexArr[ids[i]];
-        for (int q = 0; q < nstress; ++q) a->stressArr[base + q] = st[q * (size_t)m + i];
+        scatter(st.data(), (size_t)m);
       }
     }
   }
   const double *dps = c.fp32 ? c.gi32.pstrain : c.gi64.pstrain;
   const int nps = c.fp32 ? c.gi32.ne : c.gi64.ne;
   if (a->pstrain && dps) {
-    std::vector<double> ps(nps);
+    Scratch<double> ps(nps);
     EQD_CUDA_OK(cudaMemcpy(ps.data(), dps, ps.size() * 8, cudaMemcpyDeviceToHost));
 #pragma omp parallel for schedule(static)
     for (int i = 0; i < nps; ++i)
